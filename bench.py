@@ -1,0 +1,305 @@
+#!/usr/bin/env python
+"""Benchmark of the batched cloning sampler (one JSON line on rank 0).
+
+Metric: clone lattice updates per second (clone-LUPS) of the whole sampler --
+every LB step of every clone plus the cloning step -- on the workload named in
+config.workload (default: 4096 clones of a 256x64 channel, FP32 populations
+with FP64 drag integral / weights / normaliser, T = 100 LB steps per cloning
+interval).  One bench "step" is one cloning interval.
+
+  python bench.py [--steps K] [--warmup W] [--workload c3] [--impl reference]
+  torchrun --nproc-per-node N bench.py --gpus N     (independent replicas)
+
+value      device time (CUDA events on the sampler's stream) of K intervals,
+           state resident in HBM; inputs (2 x 2.4 GB population buffers) are
+           larger than L2, so no flush is needed between intervals.
+e2e        the same metric through the C ABI as a driver calls it: the initial
+           populations loaded from pinned host memory in the reference's AoS
+           FP64 layout, then per interval the drag series, labels, weights and
+           R_t read back to the host.
+roofline   the dominant kernel (the stream-collide step): algorithmic bytes
+           (72 B/LUP FP32, 144 B/LUP FP64: one read and one write of nine
+           populations) per launch / its mean duration, from CUDA event pairs
+           around the step launches inside the timed region.
+cpu_baseline the oracle's C port of the reference hot loop on this host's cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+PKG = REPO / "cloning-lbm-mpi_gb300"
+sys.path.insert(0, str(PKG))
+MEASURED_PEAKS = REPO / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path(f"/tmp/clbm_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={CLOCK_FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        v = json.loads(MEASURED_PEAKS.read_text())["hbm_gbs"]
+        return float(v), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(kernel_file: str):
+    """dram bytes per launch recorded from an ncu capture in profiles/."""
+    p = REPO / "profiles" / kernel_file
+    if not p.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch_full_size:\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl != "reference" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(wl, seconds_hint: float = 2.0):
+    """The oracle's C port of the reference hot loop (per clone: step, walls,
+    square, reset, swap, drag) on all host cores, one clone per thread; the
+    sample is ncores clones x S steps of the workload's first lattice."""
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle
+    oracle.build()
+    r = wl.runs[0]
+    g = oracle.channel_geom(r.width, r.height, r.side, r.xc, r.yc)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    t, _ = oracle.bench_lbm(g, cores, 20, r.tau, r.beta, cores)
+    per_step = t / 20
+    steps = max(20, int(seconds_hint / per_step))
+    t, _ = oracle.bench_lbm(g, cores, steps, r.tau, r.beta, cores)
+    lups = cores * r.nodes * steps
+    return {"value": lups / t, "unit": "clone-LUPS/s", "cores": cores, "kind": "port",
+            "sample": f"{cores} clones x {steps} LB steps of {r.width}x{r.height} (square {r.side}), "
+                      f"FP64, drag every step, {t:.2f} s wall"}
+
+
+def run_reference(args, wl, world, rank):
+    if rank != 0:
+        return
+    samples = [cpu_sample(wl, 1.0) for _ in range(args.warmup)]  # warm-up, discarded
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s = cpu_sample(wl, 2.0)
+        vals.append(s["value"])
+    wall = time.perf_counter() - t0
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": "clone-LUPS/s", "value": v, "unit": "clone-LUPS/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * wall / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl.name, "note": "each step is a bounded CPU sample of the workload"},
+            "cpu_baseline": {**s, "value": v},
+            "e2e": {"value": v, "unit": "clone-LUPS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10, help="timed cloning intervals")
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="c3")
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    from clbm import configs
+    wl = configs.WORKLOADS[args.workload]()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, wl, world, rank)
+        return
+
+    import torch
+    import clbm
+    torch.cuda.set_device(local)
+    s = clbm.Sampler(wl.descs(), wl.precision, max_steps=wl.steps)
+    for i, r in enumerate(wl.runs):
+        s.init_equilibrium(i, r.u0, wl.init_noise, r.seed + 1000 * rank)
+    stream = torch.cuda.ExternalStream(s.stream())
+    s.run_sampler(wl.steps, args.warmup)
+    s.sync()
+
+    # ---- timed region: K intervals, state resident in HBM ----
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.profile(True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        rv = s.run_sampler(wl.steps, args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = allmax(world, ev0.elapsed_time(ev1))
+    step_ms, nsteps = s.profile_read()
+    s.profile(False)
+    lups_interval = wl.lattice_updates_per_interval
+    value = world * lups_interval * args.steps / (ms / 1e3)
+    nodes_total = sum(r.nclones * r.nodes for r in wl.runs)
+    bpl = 72 if wl.precision == clbm.FP32 else 144
+    step_s = step_ms / 1e3 / max(1, nsteps)
+    achieved = bpl * nodes_total / step_s / 1e9
+    peak, peak_kind = hbm_peak()
+    traffic = ncu_traffic(f"k_step_{'f32' if wl.precision == clbm.FP32 else 'f64'}_{args.workload}.md")
+
+    # ---- e2e: initial load from pinned host memory + per-interval host reads ----
+    e2e = None
+    if not args.no_e2e:
+        n = [9 * r.nodes for r in wl.runs]
+        host = []
+        for i, r in enumerate(wl.runs):
+            # the reference's AoS FP64 initial states: one equilibrium field per
+            # run replicated over clones (content does not change the cost)
+            one = torch.empty(n[i], dtype=torch.float64)
+            s.dump(i, 0)  # warm the path
+            one.copy_(torch.from_numpy(s.dump(i, 0)))
+            h = one.repeat(r.nclones).pin_memory()
+            host.append(h)
+        d2h = 0
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        for i in range(len(wl.runs)):
+            clbm.check(clbm.lib().clbm_load_run_aos_f64(s.h, i, host[i].data_ptr()), "load")
+        h2d = sum(h.numel() * 8 for h in host)
+        for _ in range(args.steps):
+            s.run_interval(wl.steps)
+            for i in range(len(wl.runs)):
+                d = s.drag(i)
+                d2h += d.nbytes
+            s.clone_step()
+            for i in range(len(wl.runs)):
+                cr = s.clone_result(i)
+                d2h += cr["labels"].nbytes + cr["weights"].nbytes + 8 + cr["copies_pre"].nbytes * 2
+        torch.cuda.synchronize()
+        wall = allmax(world, time.perf_counter() - t0)
+        e2e = {"value": world * lups_interval * args.steps / wall, "unit": "clone-LUPS/s",
+               "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
+               "note": "initial AoS FP64 populations from pinned host memory (amortised over the "
+                       "steps) + per-interval drag series, labels, weights, copy numbers, R_t"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample(wl)
+    s.close()
+    if rank != 0:
+        return
+    clocks = clk.summary()
+    line = {
+        "metric": "clone-LUPS/s", "value": value, "unit": "clone-LUPS/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if wl.precision == clbm.FP32 else "f64", "data": "synthetic",
+        "config": {"workload": wl.name,
+                   "runs": [f"{r.nclones}x{r.width}x{r.height} s={r.side} k={r.k:.3f} tau={r.tau}"
+                            for r in wl.runs],
+                   "steps_per_interval": wl.steps, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (two population buffers of "
+                         f"{nodes_total * 9 * (4 if wl.precision == clbm.FP32 else 8) / 1e9:.2f} GB)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "k_step", "bytes_per_lup": bpl,
+                     "mean_step_ms": step_ms / max(1, nsteps)},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": (wl.steps + 3) * args.steps,
+        "clocks": clocks,
+        "rvalues_tail": [float(x) for x in rv[:, -1]],
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

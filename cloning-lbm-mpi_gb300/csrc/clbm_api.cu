@@ -1,0 +1,584 @@
+// clbm_api.cu -- the sampler context and the C ABI declared in include/clbm.h.
+//
+// A context owns every clone of one or several independent runs in two
+// structure-of-arrays population buffers (ping-pong), the drag-term slabs of
+// one interval, and the per-clone arrays of the cloning step.  Between
+// intervals buffer `s_buf` holds the pre-collision state S of every slot; the
+// pending labels/marks say which parent each slot copies and which slots are
+// perturbed when the next interval starts.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/clbm.h"
+#include "clbm_internal.h"
+
+using namespace clbm;
+
+static thread_local std::string g_last_error;
+
+extern "C" void clbm_set_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
+extern "C" int clbm_status_from_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return CLBM_OK;
+  g_last_error = std::string("CUDA: ") + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? CLBM_ERR_NOMEM : CLBM_ERR_CUDA;
+}
+
+#define CK(call)                                      \
+  do {                                                \
+    cudaError_t _e = (call);                          \
+    if (_e != cudaSuccess) return clbm_status_from_cuda(_e); \
+  } while (0)
+
+static int fail(int status, const char *msg) {
+  g_last_error = msg;
+  return status;
+}
+
+struct GraphEntry {
+  cudaGraphExec_t exec = nullptr;
+  int sbuf = -1, steps = -1;
+};
+
+struct clbm_ctx {
+  int nruns = 0, precision = 0, max_steps = 0, flags = 0;
+  std::vector<clbm_run_desc> desc;
+  std::vector<RunDev> runs_h;
+  int total_clones = 0, total_blocks = 0;
+  size_t pop_elems = 0, elem_size = 8;
+  void *pop[2] = {nullptr, nullptr};
+  int s_buf = 0;
+  int last_steps = 0;
+  bool any_mix = false;
+  DevArrays d{};
+  cudaStream_t stream = nullptr;
+  GraphEntry graphs[4];
+  int *d_identity = nullptr;  // 0..Nc-1 of every run, to reset pending labels
+  std::vector<char> snaps_loaded;
+  // optional timing of the step kernels: one event pair around the T step
+  // launches of every eagerly enqueued interval
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev;  // 2 per profiled interval
+  int ev_used = 0;
+  int prof_steps = 0;
+};
+
+extern "C" const char *clbm_strerror(int status) {
+  switch (status) {
+    case CLBM_OK: return "ok";
+    case CLBM_ERR_INVALID: return "invalid argument or call order";
+    case CLBM_ERR_CUDA: return "CUDA runtime error";
+    case CLBM_ERR_DEVICE: return "device error word set";
+    case CLBM_ERR_NOMEM: return "out of memory";
+    case CLBM_ERR_IO: return "I/O error";
+    case CLBM_ERR_TIMEOUT: return "bounded device wait expired";
+    default: return "unknown status";
+  }
+}
+
+extern "C" const char *clbm_last_error(void) { return g_last_error.c_str(); }
+extern "C" int clbm_version(void) { return 10000; }
+extern "C" int clbm_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+static bool geometry_ok(const clbm_run_desc &r) {
+  if (r.width < 3 || r.height < 3 || r.nclones < 1) return false;
+  if (r.xmin < 0 || r.xmax >= r.width || r.xmin > r.xmax) return false;
+  if (r.ymin < 1 || r.ymax > r.height - 2 || r.ymin > r.ymax) return false;
+  const unsigned long long nodes = (unsigned long long)r.width * r.height;
+  if ((nodes - 1) * (unsigned long long)(r.width - 1) >= (1ULL << 32)) return false;
+  return true;
+}
+
+static void destroy_graphs(clbm_ctx *c) {
+  for (auto &g : c->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = GraphEntry{};
+  }
+}
+
+extern "C" int clbm_destroy(clbm_ctx *c) {
+  if (!c) return CLBM_OK;
+  destroy_graphs(c);
+  void *bufs[] = {c->pop[0], c->pop[1], c->d.runs, c->d.state, c->d.sacc, c->d.drag, c->d.weights,
+                  c->d.labels, c->d.mark, c->d.copies_pre, c->d.copies_post, c->d.prefactors,
+                  c->d.pert, c->d.partials, c->d.scratch_i, c->d.scratch_d, c->d.snaps,
+                  c->d.rvalues, c->d.err, c->d.terms, c->d_identity};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return CLBM_OK;
+}
+
+template <typename T>
+static cudaError_t dalloc(T *&p, size_t n) {
+  if (n == 0) n = 1;
+  return cudaMalloc((void **)&p, n * sizeof(T));
+}
+
+extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, int max_steps,
+                           int flags, clbm_ctx **out) {
+  if (!out) return fail(CLBM_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!runs || nruns < 1 || nruns > 1024) return fail(CLBM_ERR_INVALID, "nruns out of range");
+  if (precision != CLBM_FP64 && precision != CLBM_FP32)
+    return fail(CLBM_ERR_INVALID, "unknown precision");
+  if (max_steps < 1) return fail(CLBM_ERR_INVALID, "max_steps < 1");
+  for (int r = 0; r < nruns; r++) {
+    const clbm_run_desc &d = runs[r];
+    if (!geometry_ok(d)) return fail(CLBM_ERR_INVALID, "invalid run geometry");
+    const int ranks = d.ranks < 1 ? 1 : d.ranks;
+    if (ranks > MAX_RANKS || d.nclones % ranks) return fail(CLBM_ERR_INVALID, "ranks must divide nclones (<= 64)");
+    if (d.perturb_mode < 0 || d.perturb_mode > 2) return fail(CLBM_ERR_INVALID, "unknown perturb_mode");
+    if (d.resample_mode < 0 || d.resample_mode > 1) return fail(CLBM_ERR_INVALID, "unknown resample_mode");
+    if (d.perturb_mode == CLBM_PERTURB_MIX && (d.nsnap < 1 || d.nsnap > MAX_SNAP))
+      return fail(CLBM_ERR_INVALID, "snapshot mix needs 1 <= nsnap <= 64");
+    if (!(d.tau > 0.5)) return fail(CLBM_ERR_INVALID, "tau must exceed 1/2");
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return fail(CLBM_ERR_CUDA, "no CUDA device");
+  }
+  clbm_ctx *c = new clbm_ctx();
+  c->nruns = nruns;
+  c->precision = precision;
+  c->max_steps = max_steps;
+  c->flags = flags;
+  c->elem_size = precision == CLBM_FP64 ? 8 : 4;
+  c->desc.assign(runs, runs + nruns);
+  c->snaps_loaded.assign(nruns, 0);
+  c->runs_h.resize(nruns);
+  long long pop = 0, terms = 0, snaps = 0;
+  int clones = 0, blocks = 0;
+  for (int r = 0; r < nruns; r++) {
+    const clbm_run_desc &d = runs[r];
+    RunDev &R = c->runs_h[r];
+    memset(&R, 0, sizeof(R));
+    R.W = d.width;
+    R.H = d.height;
+    R.xmin = d.xmin;
+    R.xmax = d.xmax;
+    R.ymin = d.ymin;
+    R.ymax = d.ymax;
+    R.nclones = d.nclones;
+    R.clone_base = clones;
+    R.block_base = blocks;
+    R.nodes = d.width * d.height;
+    R.blocks_per_clone = (R.nodes + STEP_BLOCK - 1) / STEP_BLOCK;
+    R.nterms = 2 * (d.ymax - d.ymin + 1) + 2 * (d.xmax - d.xmin + 1);
+    R.div_w = (unsigned)(((1ULL << 32) + (unsigned long long)d.width - 1) / (unsigned long long)d.width);
+    R.plane = ((long long)R.nodes + 63) / 64 * 64;
+    R.pop_base = pop;
+    R.term_base = terms;
+    R.snap_base = snaps;
+    // the reference's scalar set-up (streamCollCompute.cpp:11-12)
+    R.tau = d.tau;
+    R.omega = 1. / d.tau;
+    R.om1 = 1.0 - R.omega;
+    R.cforce = 1.0 - 0.5 * R.omega;
+    R.beta = d.beta;
+    for (int k = 0; k < 9; k++) R.wcb[k] = w_of(k) * R.cforce * d.beta;
+    R.alpha = d.alpha;
+    R.force_scale = d.force_scale;
+    R.force_shift = d.force_shift;
+    R.dt = d.dt;
+    R.eps = d.eps;
+    R.f_omega = (float)R.omega;
+    R.f_cforce = (float)R.cforce;
+    R.f_beta = (float)d.beta;
+    R.perturb_mode = d.perturb_mode;
+    R.resample_mode = d.resample_mode;
+    R.ranks = d.ranks < 1 ? 1 : d.ranks;
+    R.nsnap = d.perturb_mode == CLBM_PERTURB_MIX ? d.nsnap : 0;
+    R.seed = d.seed;
+    R.run_id = (unsigned)r;
+    pop += (long long)d.nclones * 9 * R.plane;
+    terms += (long long)R.nterms * d.nclones;
+    if (d.perturb_mode == CLBM_PERTURB_MIX) {
+      snaps += (long long)R.nsnap * 9 * R.plane;
+      c->any_mix = true;
+    }
+    clones += d.nclones;
+    blocks += d.nclones * R.blocks_per_clone;
+  }
+  c->total_clones = clones;
+  c->total_blocks = blocks;
+  c->pop_elems = (size_t)pop;
+  c->d.term_slab = terms;
+  c->d.max_steps = max_steps;
+  c->d.max_intervals = 1 << 16;
+
+  auto bail = [&](cudaError_t e) {
+    int s = clbm_status_from_cuda(e);
+    clbm_destroy(c);
+    return s;
+  };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+  for (int b = 0; b < 2; b++)
+    if ((e = cudaMalloc(&c->pop[b], c->pop_elems * c->elem_size)) != cudaSuccess) return bail(e);
+  DevArrays &D = c->d;
+  if ((e = dalloc(D.runs, nruns)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.state, nruns)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.sacc, clones)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.drag, (size_t)clones * max_steps)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.weights, clones)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.labels, clones)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.mark, clones)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.copies_pre, clones)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.copies_post, clones)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.prefactors, c->any_mix ? (size_t)clones * MAX_SNAP : 1)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.pert, 2 * (size_t)clones)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.partials, c->any_mix ? 2 * (size_t)blocks : 1)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.scratch_i, 4 * (size_t)clones + 4 * (size_t)nruns)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.scratch_d, clones)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.snaps, (size_t)snaps)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.rvalues, (size_t)nruns * D.max_intervals)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.err, 1)) != cudaSuccess) return bail(e);
+  if ((e = cudaMalloc(&D.terms, (size_t)terms * max_steps * c->elem_size)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(c->d_identity, clones)) != cudaSuccess) return bail(e);
+
+  std::vector<RunState> st(nruns);
+  std::vector<int> ident(clones);
+  for (int r = 0; r < nruns; r++) {
+    RunState &s = st[r];
+    memset(&s, 0, sizeof(s));
+    // never-seeded glibc drand48 starts at X = 0 on every rank; rank 0 runs
+    // srand(1) and discards 1000 rand() values (pops driver :176-178)
+    glibc_srand(s.rnd, 1);
+    for (int i = 0; i < 1000; i++) glibc_rand_next(s.rnd);
+    for (int j = 0; j < runs[r].nclones; j++) ident[c->runs_h[r].clone_base + j] = j;
+  }
+  cudaStream_t s = c->stream;
+  if ((e = cudaMemcpyAsync(D.runs, c->runs_h.data(), sizeof(RunDev) * nruns, cudaMemcpyHostToDevice, s)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemcpyAsync(D.state, st.data(), sizeof(RunState) * nruns, cudaMemcpyHostToDevice, s)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemcpyAsync(c->d_identity, ident.data(), sizeof(int) * clones, cudaMemcpyHostToDevice, s)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemcpyAsync(D.labels, c->d_identity, sizeof(int) * clones, cudaMemcpyDeviceToDevice, s)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemsetAsync(D.mark, 0, sizeof(int) * clones, s)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemsetAsync(D.err, 0, sizeof(unsigned), s)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemsetAsync(D.sacc, 0, sizeof(double) * clones, s)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemsetAsync(D.pert, 0, sizeof(double) * 2 * clones, s)) != cudaSuccess) return bail(e);
+  for (int b = 0; b < 2; b++)
+    if ((e = cudaMemsetAsync(c->pop[b], 0, c->pop_elems * c->elem_size, s)) != cudaSuccess) return bail(e);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return bail(e);
+  *out = c;
+  return CLBM_OK;
+}
+
+static int check_run(clbm_ctx *c, int run) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  if (run < 0 || run >= c->nruns) return fail(CLBM_ERR_INVALID, "run index out of range");
+  return CLBM_OK;
+}
+
+extern "C" int clbm_load_run_aos_f64(clbm_ctx *c, int run, const double *aos) {
+  if (int s = check_run(c, run)) return s;
+  if (!aos) return fail(CLBM_ERR_INVALID, "aos is NULL");
+  const RunDev &R = c->runs_h[run];
+  const size_t n = 9 * (size_t)R.nodes;
+  const int chunk = (int)std::max<size_t>(1, std::min<size_t>(R.nclones, (size_t)(256u << 20) / (n * 8)));
+  double *stage = nullptr;
+  CK(cudaMallocAsync((void **)&stage, n * 8 * chunk, c->stream));
+  cudaError_t e = cudaSuccess;
+  for (int c0 = 0; c0 < R.nclones && e == cudaSuccess; c0 += chunk) {
+    const int m = std::min(chunk, R.nclones - c0);
+    e = cudaMemcpyAsync(stage, aos + (size_t)c0 * n, n * 8 * m, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = launch_aos_to_soa(c->precision == CLBM_FP64, c->d.runs, run, c0, m, stage, c->pop[c->s_buf], c->stream);
+  }
+  cudaFreeAsync(stage, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return clbm_status_from_cuda(e);
+}
+
+extern "C" int clbm_load_pops_aos_f64(clbm_ctx *c, int run, int clone, const double *aos) {
+  if (int s = check_run(c, run)) return s;
+  const RunDev &R = c->runs_h[run];
+  if (clone < 0 || clone >= R.nclones || !aos) return fail(CLBM_ERR_INVALID, "bad clone or NULL array");
+  const size_t n = 9 * (size_t)R.nodes;
+  double *stage = nullptr;
+  CK(cudaMallocAsync((void **)&stage, n * 8, c->stream));
+  cudaError_t e = cudaMemcpyAsync(stage, aos, n * 8, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = launch_aos_to_soa(c->precision == CLBM_FP64, c->d.runs, run, clone, 1, stage, c->pop[c->s_buf], c->stream);
+  cudaFreeAsync(stage, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return clbm_status_from_cuda(e);
+}
+
+extern "C" int clbm_dump_pops_aos_f64(clbm_ctx *c, int run, int clone, double *aos) {
+  if (int s = check_run(c, run)) return s;
+  const RunDev &R = c->runs_h[run];
+  if (clone < 0 || clone >= R.nclones || !aos) return fail(CLBM_ERR_INVALID, "bad clone or NULL array");
+  int parent = clone;
+  CK(cudaMemcpyAsync(&parent, c->d.labels + R.clone_base + clone, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (parent < 0 || parent >= R.nclones) return fail(CLBM_ERR_DEVICE, "corrupt pending label");
+  const size_t n = 9 * (size_t)R.nodes;
+  double *stage = nullptr;
+  CK(cudaMallocAsync((void **)&stage, n * 8, c->stream));
+  cudaError_t e = launch_soa_to_aos(c->precision == CLBM_FP64, c->d.runs, run, parent, c->pop[c->s_buf], stage, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(aos, stage, n * 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(stage, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return clbm_status_from_cuda(e);
+}
+
+extern "C" int clbm_set_snapshots_aos_f64(clbm_ctx *c, int run, int nsnap, const double *aos) {
+  if (int s = check_run(c, run)) return s;
+  const RunDev &R = c->runs_h[run];
+  if (R.perturb_mode != CLBM_PERTURB_MIX) return fail(CLBM_ERR_INVALID, "run does not use the snapshot mix");
+  if (nsnap != R.nsnap || !aos) return fail(CLBM_ERR_INVALID, "nsnap differs from the run descriptor");
+  const size_t n = 9 * (size_t)R.nodes * nsnap;
+  double *stage = nullptr;
+  CK(cudaMallocAsync((void **)&stage, n * 8, c->stream));
+  cudaError_t e = cudaMemcpyAsync(stage, aos, n * 8, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = launch_snaps_to_soa(c->d.runs, run, nsnap, stage, c->d.snaps, c->stream);
+  cudaFreeAsync(stage, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) c->snaps_loaded[run] = 1;
+  return clbm_status_from_cuda(e);
+}
+
+extern "C" int clbm_init_equilibrium(clbm_ctx *c, int run, double u0, double noise,
+                                     unsigned long long seed) {
+  if (int s = check_run(c, run)) return s;
+  cudaError_t e = launch_init_equilibrium(c->precision == CLBM_FP64, c->d.runs, c->nruns, run,
+                                          c->pop[c->s_buf], u0, noise, seed, 0, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return clbm_status_from_cuda(e);
+}
+
+// Enqueue one interval on the context's stream (no synchronisation).
+// prof: record an event pair around the step launches (eager mode only).
+static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof = false) {
+  const bool f64 = c->precision == CLBM_FP64;
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+  const void *S = c->pop[sbuf];
+  if (c->any_mix) {
+    e = launch_perturb_norms(f64, c->d.runs, c->nruns, S, c->d.labels, c->d.mark, c->d.prefactors,
+                             c->d.snaps, c->d.partials, c->d.pert, c->total_blocks, c->total_clones, s);
+    if (e != cudaSuccess) return e;
+  }
+  ReseedArgs ra{c->d.runs, c->nruns, S, c->pop[1 - sbuf], c->d.labels, c->d.mark, c->d.pert,
+                c->d.prefactors, c->d.snaps, c->d.state, c->d.err};
+  if ((e = launch_reseed(f64, ra, c->total_blocks, s)) != cudaSuccess) return e;
+  int cur = 1 - sbuf;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (prof) {
+    if ((size_t)c->ev_used + 2 > c->ev.size()) {
+      for (int i = 0; i < 2; i++) {
+        cudaEvent_t ne;
+        if ((e = cudaEventCreate(&ne)) != cudaSuccess) return e;
+        c->ev.push_back(ne);
+      }
+    }
+    e0 = c->ev[c->ev_used];
+    e1 = c->ev[c->ev_used + 1];
+    c->ev_used += 2;
+    c->prof_steps += steps;
+    if ((e = cudaEventRecord(e0, s)) != cudaSuccess) return e;
+  }
+  for (int t = 0; t < steps; t++) {
+    StepArgs a{c->d.runs, c->nruns, t, c->pop[cur], c->pop[1 - cur], c->d.terms, c->d.term_slab, c->d.err};
+    if ((e = launch_step(f64, t == steps - 1, a, c->total_blocks, s)) != cudaSuccess) return e;
+    cur = 1 - cur;
+  }
+  if (prof && (e = cudaEventRecord(e1, s)) != cudaSuccess) return e;
+  if ((e = launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, s)) != cudaSuccess) return e;
+  // the pending copies and perturbations have been applied
+  if ((e = cudaMemcpyAsync(c->d.labels, c->d_identity, sizeof(int) * c->total_clones,
+                           cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+    return e;
+  return cudaMemsetAsync(c->d.mark, 0, sizeof(int) * c->total_clones, s);
+}
+
+static int check_snapshots(clbm_ctx *c) {
+  for (int r = 0; r < c->nruns; r++)
+    if (c->runs_h[r].perturb_mode == CLBM_PERTURB_MIX && !c->snaps_loaded[r])
+      return fail(CLBM_ERR_INVALID, "snapshot-mix run without snapshots (clbm_set_snapshots_aos_f64)");
+  return CLBM_OK;
+}
+
+static int sbuf_after(int sbuf, int steps) {
+  // reseed writes P into 1-sbuf, each step flips; the last step writes S
+  return (steps % 2 == 0) ? sbuf : 1 - sbuf;
+}
+
+extern "C" int clbm_run_interval(clbm_ctx *c, int steps) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  if (steps < 1 || steps > c->max_steps) return fail(CLBM_ERR_INVALID, "steps outside [1, max_steps]");
+  if (int st = check_snapshots(c)) return st;
+  CK(enqueue_interval(c, steps, c->s_buf, c->profiling));
+  c->s_buf = sbuf_after(c->s_buf, steps);
+  c->last_steps = steps;
+  return CLBM_OK;
+}
+
+static int check_error_word(clbm_ctx *c) {
+  unsigned w = 0;
+  CK(cudaMemcpyAsync(&w, c->d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (w) {
+    char msg[96];
+    snprintf(msg, sizeof msg, "device error word 0x%x", w);
+    return fail(CLBM_ERR_DEVICE, msg);
+  }
+  return CLBM_OK;
+}
+
+extern "C" int clbm_clone_step(clbm_ctx *c) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  if (c->last_steps < 1) return fail(CLBM_ERR_INVALID, "clone step before any interval");
+  CK(launch_clone(c->d, c->nruns, c->stream));
+  return check_error_word(c);
+}
+
+extern "C" int clbm_get_drag(clbm_ctx *c, int run, double *out) {
+  if (int s = check_run(c, run)) return s;
+  if (!out) return fail(CLBM_ERR_INVALID, "out is NULL");
+  if (c->last_steps < 1) return fail(CLBM_ERR_INVALID, "no interval has run");
+  const RunDev &R = c->runs_h[run];
+  CK(cudaMemcpy2DAsync(out, sizeof(double) * c->last_steps, c->d.drag + (size_t)R.clone_base * c->max_steps,
+                       sizeof(double) * c->max_steps, sizeof(double) * c->last_steps, R.nclones,
+                       cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return CLBM_OK;
+}
+
+extern "C" int clbm_get_clone_result(clbm_ctx *c, int run, int *labels, double *rvalue,
+                                     double *weights, int *copies_pre, int *copies_post) {
+  if (int s = check_run(c, run)) return s;
+  const RunDev &R = c->runs_h[run];
+  const size_t nc = R.nclones, g0 = R.clone_base;
+  cudaStream_t s = c->stream;
+  if (labels) CK(cudaMemcpyAsync(labels, c->d.labels + g0, nc * sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (weights) CK(cudaMemcpyAsync(weights, c->d.weights + g0, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (copies_pre) CK(cudaMemcpyAsync(copies_pre, c->d.copies_pre + g0, nc * sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (copies_post) CK(cudaMemcpyAsync(copies_post, c->d.copies_post + g0, nc * sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (rvalue) CK(cudaMemcpyAsync(rvalue, &c->d.state[run].rbar, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return CLBM_OK;
+}
+
+static int graph_for(clbm_ctx *c, int steps, int sbuf, cudaGraphExec_t *exec) {
+  for (auto &g : c->graphs)
+    if (g.exec && g.sbuf == sbuf && g.steps == steps) {
+      *exec = g.exec;
+      return CLBM_OK;
+    }
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = enqueue_interval(c, steps, sbuf);
+  if (e == cudaSuccess) e = launch_clone(c->d, c->nruns, c->stream);
+  cudaError_t e2 = cudaStreamEndCapture(c->stream, &graph);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return clbm_status_from_cuda(e);
+  }
+  cudaGraphExec_t ge = nullptr;
+  e = cudaGraphInstantiate(&ge, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return clbm_status_from_cuda(e);
+  GraphEntry *slot = nullptr;
+  for (auto &g : c->graphs)
+    if (!g.exec) {
+      slot = &g;
+      break;
+    }
+  if (!slot) {
+    destroy_graphs(c);
+    slot = &c->graphs[0];
+  }
+  slot->exec = ge;
+  slot->sbuf = sbuf;
+  slot->steps = steps;
+  *exec = ge;
+  return CLBM_OK;
+}
+
+extern "C" int clbm_run_sampler(clbm_ctx *c, int steps, int intervals, double *rvalues) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  if (steps < 1 || steps > c->max_steps || intervals < 0) return fail(CLBM_ERR_INVALID, "bad steps/intervals");
+  if (int st = check_snapshots(c)) return st;
+  for (int i = 0; i < intervals; i++) {
+    if ((c->flags & CLBM_FLAG_GRAPH) && !c->profiling) {
+      cudaGraphExec_t ge = nullptr;
+      if (int st = graph_for(c, steps, c->s_buf, &ge)) return st;
+      CK(cudaGraphLaunch(ge, c->stream));
+    } else {
+      CK(enqueue_interval(c, steps, c->s_buf, c->profiling));
+      CK(launch_clone(c->d, c->nruns, c->stream));
+    }
+    c->s_buf = sbuf_after(c->s_buf, steps);
+    c->last_steps = steps;
+  }
+  if (int st = check_error_word(c)) return st;
+  if (rvalues && intervals > 0) {
+    for (int r = 0; r < c->nruns; r++) {
+      int f = 0;
+      CK(cudaMemcpyAsync(&f, &c->d.state[r].interval, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      f -= intervals;
+      if (f < 0 || f + intervals > c->d.max_intervals) return fail(CLBM_ERR_INVALID, "R_t history capacity exceeded");
+      CK(cudaMemcpyAsync(rvalues + (size_t)r * intervals, c->d.rvalues + (size_t)r * c->d.max_intervals + f,
+                         sizeof(double) * intervals, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return CLBM_OK;
+}
+
+extern "C" int clbm_error_word(clbm_ctx *c, unsigned *word, int clear) {
+  if (!c || !word) return fail(CLBM_ERR_INVALID, "NULL argument");
+  CK(cudaMemcpyAsync(word, c->d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  if (clear) CK(cudaMemsetAsync(c->d.err, 0, sizeof(unsigned), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return CLBM_OK;
+}
+
+extern "C" int clbm_sync(clbm_ctx *c) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  CK(cudaStreamSynchronize(c->stream));
+  return CLBM_OK;
+}
+
+extern "C" void *clbm_stream(clbm_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+extern "C" int clbm_profile(clbm_ctx *c, int enable) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  c->profiling = enable != 0;
+  c->ev_used = 0;
+  c->prof_steps = 0;
+  return CLBM_OK;
+}
+
+extern "C" int clbm_profile_read(clbm_ctx *c, double *step_ms, int *nsteps) {
+  if (!c || !step_ms || !nsteps) return fail(CLBM_ERR_INVALID, "NULL argument");
+  CK(cudaStreamSynchronize(c->stream));
+  double total = 0.0;
+  for (int i = 0; i + 1 < c->ev_used; i += 2) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev[i], c->ev[i + 1]));
+    total += ms;
+  }
+  *step_ms = total;
+  *nsteps = c->prof_steps;
+  c->ev_used = 0;
+  c->prof_steps = 0;
+  return CLBM_OK;
+}

@@ -1,0 +1,98 @@
+// clbm_internal.h -- structures shared by the kernel translation units and the
+// host-side context (clbm_api.cu).  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "clbm_common.cuh"
+
+namespace clbm {
+
+constexpr int MAX_RANKS = 64;   // virtual MPI ranks per run
+constexpr int MAX_SNAP = 64;    // perturbation snapshots per run
+constexpr int STEP_BLOCK = 256; // nodes per block of the step kernels
+
+// Per-run state that lives on the device between kernels (random-stream
+// positions, interval counter), so that captured CUDA graphs replay with the
+// state advancing on the device.
+struct RunState {
+  unsigned long long d48[MAX_RANKS];  // drand48 X of each virtual rank
+  GlibcRand rnd;                      // rank 0's glibc rand() state
+  int interval;                       // cloning intervals completed
+  int ncomm;                          // clone copies of the last clone step
+  int ncopies_drawn;                  // NcPrime of the last clone step
+  int pad_;
+  double rbar;                        // R_t of the last clone step
+};
+
+// Device arrays of one context (all indexed by global clone index unless
+// stated otherwise).
+struct DevArrays {
+  RunDev *runs;       // [nruns]
+  RunState *state;    // [nruns]
+  double *sacc;       // weight integral s_j = dt * sum F of the last interval
+  double *drag;       // per run: [nclones][max_steps] F values, run base = clone_base*max_steps
+  double *weights;    // exp(alpha s_j) (reference) / exp(alpha s_j) (systematic)
+  int *labels;        // parent slot (run-local) of each slot, pending until the next interval
+  int *mark;          // 1 = slot receives a copy and is perturbed at the next interval
+  int *copies_pre;    // copy numbers drawn
+  int *copies_post;   // after the kill/duplicate correction
+  double *prefactors; // [clone][MAX_SNAP] snapshot-mix prefactors of marked clones
+  double *pert;       // [clone][2] (weight, 1/a) of the snapshot mix
+  double *partials;   // [clone][blocks_per_clone][2] norm partial sums
+  int *scratch_i;     // per run: 4*nclones+4 ints (copy numbers, sampling array, extras)
+  double *scratch_d;  // per run: nclones doubles (prefix sums)
+  double *snaps;      // per run: nsnap * 9 * plane FP64, SoA like the populations
+  double *rvalues;    // per run: [max_intervals] R_t history
+  unsigned *err;      // device error word
+  void *terms;        // [max_steps][slab] drag terms (double or float)
+  long long term_slab;// terms per step over all runs
+  int max_steps;
+  int max_intervals;
+};
+
+struct StepArgs {
+  const RunDev *runs;
+  int nruns;
+  int step;           // step index within the interval (drag-term slab)
+  const void *src;    // post-collision populations of the previous step
+  void *dst;          // this step's post-collision (or, on the last step, pre-collision) populations
+  void *terms;        // base of the term slabs
+  long long term_slab;
+  unsigned *err;
+};
+
+struct ReseedArgs {
+  const RunDev *runs;
+  int nruns;
+  const void *src;    // pre-collision state S of every slot's parent
+  void *dst;          // post-collision populations P of the next interval's first step
+  const int *labels;
+  const int *mark;
+  const double *pert;       // (weight, 1/a) per clone
+  const double *prefactors; // [clone][MAX_SNAP]
+  const double *snaps;
+  const RunState *state;    // interval counter
+  unsigned *err;
+};
+
+// kernel launchers (clbm_step.cu, clbm_cloning.cu)
+cudaError_t launch_step(bool f64, bool last, const StepArgs &a, int blocks, cudaStream_t s);
+cudaError_t launch_reseed(bool f64, const ReseedArgs &a, int blocks, cudaStream_t s);
+cudaError_t launch_perturb_norms(bool f64, const RunDev *runs, int nruns, const void *src,
+                                 const int *labels, const int *mark, const double *prefactors,
+                                 const double *snaps, double *partials, double *pert,
+                                 int blocks, int total_clones, cudaStream_t s);
+cudaError_t launch_drag_reduce(bool f64, const DevArrays &d, int nruns, int total_clones,
+                               int steps, cudaStream_t s);
+cudaError_t launch_clone(const DevArrays &d, int nruns, cudaStream_t s);
+cudaError_t launch_init_equilibrium(bool f64, const RunDev *runs, int nruns, int run, void *pop,
+                                    double u0, double noise, unsigned long long seed, int blocks,
+                                    cudaStream_t s);
+cudaError_t launch_aos_to_soa(bool f64, const RunDev *runs, int run, int clone0, int nclone,
+                              const double *aos, void *pop, cudaStream_t s);
+cudaError_t launch_soa_to_aos(bool f64, const RunDev *runs, int run, int clone, const void *pop,
+                              double *aos, cudaStream_t s);
+cudaError_t launch_snaps_to_soa(const RunDev *runs, int run, int nsnap, const double *aos,
+                                double *snaps, cudaStream_t s);
+
+}  // namespace clbm

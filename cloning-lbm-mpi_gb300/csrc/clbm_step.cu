@@ -1,0 +1,477 @@
+// clbm_step.cu -- the batched stream-collide step and the kernels that prepare
+// an interval (copy + perturbation + first collision), all over the
+// structure-of-arrays population buffer of every clone of every run.
+//
+// Buffer semantics ("pull" scheme).  Between steps the buffer holds the
+// POST-collision populations P of every fluid node.  Step t reads P_t,
+// gathers the streamed state S_{t+1}(n,k) = P_t(n - c_k, k) -- or, where the
+// reference bounces the slot back, the node's own P_t(n, opp k) -- resets
+// square-interior nodes to w[k], evaluates the drag terms of S_{t+1} on the
+// square perimeter, collides and writes P_{t+1}.  This is the reference's
+// collide -> push-stream -> wall BB -> square BB -> interior reset -> swap
+// -> drag sequence (src/mpi_LBM_GK_pops_perturb.cpp:426-445) with the time
+// origin moved by half a step, so each node is read and written exactly once
+// per step with aligned stores.  The last step of an interval writes S instead
+// of P, because the cloning step and the perturbation act on S.
+#include <cstdint>
+
+#include "clbm_internal.h"
+#include "clbm_physics.cuh"
+
+namespace clbm {
+
+__device__ __forceinline__ int find_run_by_block(const RunDev *runs, int nruns, int b) {
+  int r = 0;
+  while (r + 1 < nruns && b >= runs[r + 1].block_base) r++;
+  return r;
+}
+
+struct NodeLoc {
+  int run, clone, n, x, y;
+  bool valid;
+};
+
+__device__ __forceinline__ NodeLoc locate(const RunDev *runs, int nruns) {
+  NodeLoc L;
+  const int b = blockIdx.x;
+  L.run = find_run_by_block(runs, nruns, b);
+  const RunDev &R = runs[L.run];
+  const int local = b - R.block_base;
+  L.clone = local / R.blocks_per_clone;
+  const int tile = local - L.clone * R.blocks_per_clone;
+  L.n = tile * blockDim.x + threadIdx.x;
+  L.valid = L.n < R.nodes && L.clone < R.nclones;
+  L.y = (int)__umulhi((unsigned)L.n, R.div_w);
+  L.x = L.n - L.y * R.W;
+  return L;
+}
+
+template <bool F64>
+using pop_t = typename std::conditional<F64, double, float>::type;
+
+// Drag terms of one perimeter node, stored at [term][clone] so that the
+// reduction reads them coalesced: West (x = xmin, index y - ymin), East,
+// North (y = ymax, index x - xmin), South.  FP64: the reference's per-node
+// expressions (force.cpp:48, :78, :108, :138).  FP32: shifted variant without
+// the +-1/3 that cancel between West and East.
+template <bool F64>
+__device__ __forceinline__ void store_drag_terms(const RunDev &R, const pop_t<F64> S[9],
+                                                 int x, int y, int clone, pop_t<F64> *T) {
+  const int sy = R.ymax - R.ymin, sx = R.xmax - R.xmin;
+  const int nc = R.nclones;
+  pop_t<F64> west, east, north, south;
+  if constexpr (F64) {
+    double rho, pxx, pxy;
+    pi_ref64(S, rho, pxx, pxy);
+    const double third = 1. / 3.;
+    const double c = R.cforce;
+    west = DADD(DMUL(rho, third), DMUL(c, pxx));
+    east = DSUB(DMUL(-rho, third), DMUL(c, pxx));
+    north = DMUL(-c, pxy);
+    south = DMUL(c, pxy);
+  } else {
+    float drho, pxx, pxy;
+    pi_f32(S, drho, pxx, pxy);
+    const float c = R.f_cforce;
+    west = drho * (1.0f / 3.0f) + c * pxx;
+    east = -west;
+    north = -c * pxy;
+    south = c * pxy;
+  }
+  if (x == R.xmin) T[(long long)(y - R.ymin) * nc + clone] = west;
+  if (x == R.xmax) T[(long long)(sy + 1 + y - R.ymin) * nc + clone] = east;
+  if (y == R.ymax) T[(long long)(2 * (sy + 1) + x - R.xmin) * nc + clone] = north;
+  if (y == R.ymin) T[(long long)(2 * (sy + 1) + sx + 1 + x - R.xmin) * nc + clone] = south;
+}
+
+template <bool F64>
+__device__ __forceinline__ void collide_node(const RunDev &R, const pop_t<F64> S[9],
+                                             pop_t<F64> P[9]) {
+  if constexpr (F64) {
+    collide_ref64(S, P, R.beta, R.wcb, R.omega, R.om1);
+  } else {
+    collide_f32(S, P, R.f_beta, R.f_omega, R.f_cforce);
+  }
+}
+
+template <bool F64>
+__device__ __forceinline__ bool density_ok(const pop_t<F64> S[9]) {
+  if constexpr (F64) {
+    double r = S[0];
+#pragma unroll
+    for (int k = 1; k < 9; k++) r += S[k];
+    return r > 0.0;
+  } else {
+    float d = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; k++) d += S[k];
+    return d > -1.0f;
+  }
+}
+
+template <bool F64, bool LAST>
+__global__ void __launch_bounds__(STEP_BLOCK) k_step(StepArgs a) {
+  using T = pop_t<F64>;
+  const NodeLoc L = locate(a.runs, a.nruns);
+  if (!L.valid) return;
+  const RunDev &R = a.runs[L.run];
+  const long long plane = R.plane;
+  const long long cbase = R.pop_base + (long long)L.clone * 9 * plane;
+  const T *__restrict__ src = (const T *)a.src + cbase;
+  T *__restrict__ dst = (T *)a.dst + cbase;
+  const int x = L.x, y = L.y, n = L.n, W = R.W;
+
+  const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+  const int mask = (in_box || y == 0 || y == R.H - 1) ? bounce_mask(R, x, y) : 0;
+  if (mask & 512) {
+    // inside the square: reset to w[k] (stored shifted as 0 in FP32); its
+    // post-collision values are never pulled by a fluid node
+    if (LAST) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) dst[k * plane + n] = F64 ? (T)w_of(k) : (T)0;
+    }
+    return;
+  }
+  const int xl = (x == 0) ? W - 1 : x - 1;
+  const int xr = (x == W - 1) ? 0 : x + 1;
+  const int row = y * W;
+  T S[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const int cx = cx_of(k), cy = cy_of(k);
+    const int sx = cx == 1 ? xl : (cx == -1 ? xr : x);
+    const int srow = cy == 1 ? row - W : (cy == -1 ? row + W : row);
+    const T *p = ((mask >> k) & 1) ? src + opp_of(k) * plane + n : src + k * plane + srow + sx;
+    S[k] = __ldg(p);
+  }
+  if (in_box) {
+    T *terms = (T *)a.terms + (long long)a.step * a.term_slab + R.term_base;
+    store_drag_terms<F64>(R, S, x, y, L.clone, terms);
+  }
+  if (!density_ok<F64>(S)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
+  if (LAST) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) dst[k * plane + n] = S[k];
+  } else {
+    T P[9];
+    collide_node<F64>(R, S, P);
+#pragma unroll
+    for (int k = 0; k < 9; k++) dst[k * plane + n] = P[k];
+  }
+}
+
+cudaError_t launch_step(bool f64, bool last, const StepArgs &a, int blocks, cudaStream_t s) {
+  if (f64) {
+    if (last)
+      k_step<true, true><<<blocks, STEP_BLOCK, 0, s>>>(a);
+    else
+      k_step<true, false><<<blocks, STEP_BLOCK, 0, s>>>(a);
+  } else {
+    if (last)
+      k_step<false, true><<<blocks, STEP_BLOCK, 0, s>>>(a);
+    else
+      k_step<false, false><<<blocks, STEP_BLOCK, 0, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Reseed: the first kernel of an interval.  Slot j takes its parent's state
+// S(labels[j]) (the clone copy, pops driver :658-701), new clones are
+// perturbed (:412-416: snapshot mix, generatePerturbedState.cpp:4-38, or the
+// counter-based uniform noise), and the result is collided into P.
+__device__ __forceinline__ uint32_t aos_index(const RunDev &R, int x, int y, int k) {
+  return (uint32_t)(k + 9 * (y + R.H * x));
+}
+
+template <bool F64>
+__global__ void __launch_bounds__(STEP_BLOCK) k_reseed(ReseedArgs a) {
+  using T = pop_t<F64>;
+  const NodeLoc L = locate(a.runs, a.nruns);
+  if (!L.valid) return;
+  const RunDev &R = a.runs[L.run];
+  const int x = L.x, y = L.y, n = L.n;
+  const bool solid = x > R.xmin && x < R.xmax && y > R.ymin && y < R.ymax;
+  if (solid) return;  // post-collision values of interior nodes are never pulled
+  const int gclone = R.clone_base + L.clone;
+  int parent = a.labels[gclone];
+  if (parent < 0 || parent >= R.nclones) {
+    atomicOr(a.err, (unsigned)ERR_BAD_PARENT);
+    parent = L.clone;
+  }
+  const long long plane = R.plane;
+  const T *src = (const T *)a.src + R.pop_base + (long long)parent * 9 * plane;
+  T *dst = (T *)a.dst + R.pop_base + (long long)L.clone * 9 * plane;
+  T S[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) S[k] = src[k * plane + n];
+  if (R.perturb_mode != 0 && a.mark[gclone]) {
+    const int interval = a.state[L.run].interval;
+    const double *pre = a.prefactors + (long long)gclone * MAX_SNAP;
+    const double wgt = a.pert[2 * gclone], inv_a = a.pert[2 * gclone + 1];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      double f = F64 ? (double)S[k] : w_of(k) + (double)S[k];
+      if (R.perturb_mode == 2) {
+        const double u = philox_uniform(R.seed, aos_index(R, x, y, k), (uint32_t)L.clone,
+                                        (uint32_t)interval, (R.run_id << 4) | DOM_PERTURB);
+        f = DMUL(f, DADD(1.0, DMUL(R.eps, DSUB(DMUL(2.0, u), 1.0))));
+      } else {
+        // S = sum_q r_q snap_q in snapshot order; f <- (f + eps*S*weight) / a
+        const double *sp = a.snaps + R.snap_base + (long long)k * plane + n;
+        double mix = DMUL(pre[0], sp[0]);
+        for (int q = 1; q < R.nsnap; q++) mix = DADD(mix, DMUL(pre[q], sp[(long long)q * 9 * plane]));
+        f = DMUL(DADD(f, DMUL(DMUL(R.eps, mix), wgt)), inv_a);
+      }
+      S[k] = F64 ? (T)f : (T)(f - w_of(k));
+    }
+  }
+  T P[9];
+  collide_node<F64>(R, S, P);
+#pragma unroll
+  for (int k = 0; k < 9; k++) dst[k * plane + n] = P[k];
+}
+
+cudaError_t launch_reseed(bool f64, const ReseedArgs &a, int blocks, cudaStream_t s) {
+  if (f64)
+    k_reseed<true><<<blocks, STEP_BLOCK, 0, s>>>(a);
+  else
+    k_reseed<false><<<blocks, STEP_BLOCK, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Norms of the snapshot-mix perturbation (generatePerturbedState.cpp:22-31):
+// |f|^2 of the parent state and |sum_q r_q snap_q|^2 over all 9*Dx*Dy values.
+// Each block reduces its nodes in a fixed tree order into partials[block];
+// the finalize kernel adds the blocks of a clone in order.  (The reference
+// adds all values sequentially; the fixed tree order differs from it only in
+// the rounding of the two norms.)
+template <bool F64>
+__global__ void __launch_bounds__(STEP_BLOCK)
+    k_perturb_norms(const RunDev *runs, int nruns, const void *srcv, const int *labels,
+                    const int *mark, const double *prefactors, const double *snaps,
+                    double *partials) {
+  using T = pop_t<F64>;
+  __shared__ double red[2][STEP_BLOCK / 32];
+  const NodeLoc L = locate(runs, nruns);
+  const RunDev &R = runs[L.run];
+  const int gclone = R.clone_base + L.clone;
+  // whole block exits together (one clone per block)
+  if (L.clone >= R.nclones || R.perturb_mode != 1 || !mark[gclone]) return;
+  double n0 = 0.0, n1 = 0.0;
+  if (L.n < R.nodes) {
+    const int parent = labels[gclone];
+    const long long plane = R.plane;
+    const T *src = (const T *)srcv + R.pop_base + (long long)parent * 9 * plane;
+    const double *pre = prefactors + (long long)gclone * MAX_SNAP;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      const double f = F64 ? (double)src[k * plane + L.n] : w_of(k) + (double)src[k * plane + L.n];
+      const double *sp = snaps + R.snap_base + (long long)k * plane + L.n;
+      double mix = DMUL(pre[0], sp[0]);
+      for (int q = 1; q < R.nsnap; q++) mix = DADD(mix, DMUL(pre[q], sp[(long long)q * 9 * plane]));
+      n0 = DADD(n0, DMUL(f, f));
+      n1 = DADD(n1, DMUL(mix, mix));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    n0 = DADD(n0, __shfl_down_sync(0xffffffffu, n0, o));
+    n1 = DADD(n1, __shfl_down_sync(0xffffffffu, n1, o));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][warp] = n0;
+    red[1][warp] = n1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a0 = red[0][0], a1 = red[1][0];
+    for (int i = 1; i < STEP_BLOCK / 32; i++) {
+      a0 = DADD(a0, red[0][i]);
+      a1 = DADD(a1, red[1][i]);
+    }
+    partials[2 * (long long)blockIdx.x] = a0;
+    partials[2 * (long long)blockIdx.x + 1] = a1;
+  }
+}
+
+__global__ void k_perturb_finalize(const RunDev *runs, int nruns, const int *mark,
+                                   const double *prefactors, const double *partials,
+                                   double *pert, int total_clones) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total_clones) return;
+  int r = 0;
+  while (r + 1 < nruns && g >= runs[r + 1].clone_base) r++;
+  const RunDev &R = runs[r];
+  if (!mark[g] || R.perturb_mode != 1) return;
+  const int c = g - R.clone_base;
+  const long long b0 = R.block_base + (long long)c * R.blocks_per_clone;
+  double n0 = partials[2 * b0], n1 = partials[2 * b0 + 1];
+  for (int t = 1; t < R.blocks_per_clone; t++) {
+    n0 = DADD(n0, partials[2 * (b0 + t)]);
+    n1 = DADD(n1, partials[2 * (b0 + t) + 1]);
+  }
+  n0 = __dsqrt_rn(n0);
+  n1 = __dsqrt_rn(n1);
+  const double weight = DDIV(n0, n1);
+  const double *pre = prefactors + (long long)g * MAX_SNAP;
+  double sum = pre[0];
+  for (int q = 1; q < R.nsnap; q++) sum = DADD(sum, pre[q]);
+  const double a = DADD(1.0, DMUL(DMUL(sum, R.eps), weight));
+  pert[2 * g] = weight;
+  pert[2 * g + 1] = DDIV(1., a);
+}
+
+cudaError_t launch_perturb_norms(bool f64, const RunDev *runs, int nruns, const void *src,
+                                 const int *labels, const int *mark, const double *prefactors,
+                                 const double *snaps, double *partials, double *pert,
+                                 int blocks, int total_clones, cudaStream_t s) {
+  if (f64)
+    k_perturb_norms<true><<<blocks, STEP_BLOCK, 0, s>>>(runs, nruns, src, labels, mark,
+                                                         prefactors, snaps, partials);
+  else
+    k_perturb_norms<false><<<blocks, STEP_BLOCK, 0, s>>>(runs, nruns, src, labels, mark,
+                                                          prefactors, snaps, partials);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_perturb_finalize<<<(total_clones + 255) / 256, 256, 0, s>>>(runs, nruns, mark, prefactors,
+                                                                 partials, pert, total_clones);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Synthetic initial state, the same arithmetic as the oracle's
+// orc_init_equilibrium: feq(rho=1, u=(u0,0)) * (1 + noise (2u - 1)) in the
+// fluid, w[k] inside the square; stored as the pre-collision state S.
+template <bool F64>
+__global__ void __launch_bounds__(STEP_BLOCK)
+    k_init_equilibrium(const RunDev *runs, int nruns, int run, void *popv, double u0,
+                       double noise, unsigned long long seed) {
+  using T = pop_t<F64>;
+  const RunDev &R = runs[run];
+  const int clone = blockIdx.y;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= R.nodes || clone >= R.nclones) return;
+  const int y = n / R.W, x = n - y * R.W;
+  const bool solid = x > R.xmin && x < R.xmax && y > R.ymin && y < R.ymax;
+  T *pop = (T *)popv + R.pop_base + (long long)clone * 9 * R.plane;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    double f;
+    if (solid) {
+      f = w_of(k);
+    } else {
+      const double eu = DMUL((double)cx_of(k), u0);
+      const double feq = DMUL(w_of(k), DADD(DADD(DADD(1.0, DMUL(3.0, eu)), DMUL(DMUL(4.5, eu), eu)),
+                                            DMUL(-1.5, DMUL(u0, u0))));
+      const double u = philox_uniform(seed, aos_index(R, x, y, k), (uint32_t)clone, 0xFFFFFFFFu,
+                                      (R.run_id << 4) | DOM_INIT);
+      f = DMUL(feq, DADD(1.0, DMUL(noise, DSUB(DMUL(2.0, u), 1.0))));
+    }
+    pop[k * R.plane + n] = F64 ? (T)f : (T)(f - w_of(k));
+  }
+}
+
+cudaError_t launch_init_equilibrium(bool f64, const RunDev *runs, int nruns, int run, void *pop,
+                                    double u0, double noise, unsigned long long seed, int blocks,
+                                    cudaStream_t s) {
+  (void)blocks;
+  RunDev h;
+  cudaError_t e = cudaMemcpyAsync(&h, runs + run, sizeof(RunDev), cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  dim3 grid((h.nodes + 255) / 256, h.nclones);
+  if (f64)
+    k_init_equilibrium<true><<<grid, 256, 0, s>>>(runs, nruns, run, pop, u0, noise, seed);
+  else
+    k_init_equilibrium<false><<<grid, 256, 0, s>>>(runs, nruns, run, pop, u0, noise, seed);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Layout conversion between the reference's AoS FP64 files/arrays
+// (k + 9*(y + Dy*x)) and the device SoA buffer (plane k, node y*Dx + x).
+template <bool F64>
+__global__ void k_aos_to_soa(const RunDev *runs, int run, int clone0, const double *aos,
+                             void *popv) {
+  using T = pop_t<F64>;
+  const RunDev &R = runs[run];
+  const int c = blockIdx.y;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // AoS node order: t = y + H*x
+  if (t >= R.nodes) return;
+  const int x = t / R.H, y = t - x * R.H;
+  const double *src = aos + (long long)c * 9 * R.nodes + 9LL * t;
+  T *dst = (T *)popv + R.pop_base + (long long)(clone0 + c) * 9 * R.plane + (long long)y * R.W + x;
+#pragma unroll
+  for (int k = 0; k < 9; k++) dst[k * R.plane] = F64 ? (T)src[k] : (T)(src[k] - w_of(k));
+}
+
+template <bool F64>
+__global__ void k_soa_to_aos(const RunDev *runs, int run, int clone, const void *popv,
+                             double *aos) {
+  using T = pop_t<F64>;
+  const RunDev &R = runs[run];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= R.nodes) return;
+  const int x = t / R.H, y = t - x * R.H;
+  const T *src = (const T *)popv + R.pop_base + (long long)clone * 9 * R.plane + (long long)y * R.W + x;
+#pragma unroll
+  for (int k = 0; k < 9; k++) aos[9LL * t + k] = F64 ? (double)src[k * R.plane] : w_of(k) + (double)src[k * R.plane];
+}
+
+__global__ void k_snaps_to_soa(const RunDev *runs, int run, const double *aos, double *snaps) {
+  const RunDev &R = runs[run];
+  const int q = blockIdx.y;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= R.nodes) return;
+  const int x = t / R.H, y = t - x * R.H;
+  const double *src = aos + (long long)q * 9 * R.nodes + 9LL * t;
+  double *dst = snaps + R.snap_base + (long long)q * 9 * R.plane + (long long)y * R.W + x;
+#pragma unroll
+  for (int k = 0; k < 9; k++) dst[k * R.plane] = src[k];
+}
+
+static cudaError_t run_geometry(const RunDev *runs, int run, RunDev &h, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyAsync(&h, runs + run, sizeof(RunDev), cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(s);
+}
+
+cudaError_t launch_aos_to_soa(bool f64, const RunDev *runs, int run, int clone0, int nclone,
+                              const double *aos, void *pop, cudaStream_t s) {
+  RunDev h;
+  cudaError_t e = run_geometry(runs, run, h, s);
+  if (e != cudaSuccess) return e;
+  dim3 grid((h.nodes + 255) / 256, nclone);
+  if (f64)
+    k_aos_to_soa<true><<<grid, 256, 0, s>>>(runs, run, clone0, aos, pop);
+  else
+    k_aos_to_soa<false><<<grid, 256, 0, s>>>(runs, run, clone0, aos, pop);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_soa_to_aos(bool f64, const RunDev *runs, int run, int clone, const void *pop,
+                              double *aos, cudaStream_t s) {
+  RunDev h;
+  cudaError_t e = run_geometry(runs, run, h, s);
+  if (e != cudaSuccess) return e;
+  if (f64)
+    k_soa_to_aos<true><<<(h.nodes + 255) / 256, 256, 0, s>>>(runs, run, clone, pop, aos);
+  else
+    k_soa_to_aos<false><<<(h.nodes + 255) / 256, 256, 0, s>>>(runs, run, clone, pop, aos);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_snaps_to_soa(const RunDev *runs, int run, int nsnap, const double *aos,
+                                double *snaps, cudaStream_t s) {
+  RunDev h;
+  cudaError_t e = run_geometry(runs, run, h, s);
+  if (e != cudaSuccess) return e;
+  dim3 grid((h.nodes + 255) / 256, nsnap);
+  k_snaps_to_soa<<<grid, 256, 0, s>>>(runs, run, aos, snaps);
+  return cudaGetLastError();
+}
+
+}  // namespace clbm

@@ -1,0 +1,211 @@
+/*
+ * clbm.h -- C ABI of libclbm, the GB300-native cloning sampler over D2Q9
+ * lattice-Boltzmann clones of a body-force-driven channel flow past a square.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and
+ * returns an int status (CLBM_OK == 0, negative on error; clbm_strerror and
+ * clbm_last_error describe it).  There is no CPU fallback: without a CUDA
+ * device the calls that compute return CLBM_ERR_CUDA.
+ *
+ * Two levels, mirroring the reference (tlestang/cloning-lbm-MPI):
+ *
+ *  1. Function level (clbm_ref_*): one clone in the reference's own FP64
+ *     array-of-structures layout IDX(x,y,k) = k + 9*(y + Dy*x)
+ *     (src/lbm_src/global.h:4), DEVICE pointers, geometry passed explicitly
+ *     instead of through the reference's globals Dx, Dy, xmin, xmax, ymin, ymax
+ *     (src/lbm_src/global.h:11-13).  Results are bit-identical to the
+ *     reference functions named beside each declaration.
+ *
+ *  2. Sampler level (clbm_ctx): every clone of one or several independent runs
+ *     lives in one device-resident structure-of-arrays population buffer; one
+ *     call advances them all by a cloning interval, one call performs the
+ *     cloning step (weights, normaliser, resampling, clone copy,
+ *     perturbation of new clones).  This replaces the MPI drivers' per-rank
+ *     clone loops and point-to-point clone transfers
+ *     (src/mpi_LBM_GK_pops_perturb.cpp:387-701).
+ *
+ * Threading: a context is used by one host thread at a time; its work is
+ * ordered on the context's own CUDA stream.
+ */
+#ifndef CLBM_H
+#define CLBM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define CLBM_OK 0
+#define CLBM_ERR_INVALID (-1) /* bad argument or call order */
+#define CLBM_ERR_CUDA (-2)    /* CUDA runtime error, or no device */
+#define CLBM_ERR_DEVICE (-3)  /* the device error word was set (see below) */
+#define CLBM_ERR_NOMEM (-4)   /* device or pinned host allocation failed */
+#define CLBM_ERR_IO (-5)      /* file I/O (drivers) */
+#define CLBM_ERR_TIMEOUT (-6) /* a bounded device wait gave up */
+
+/* device error word bits (clbm_error_word) */
+#define CLBM_DEV_NONFINITE_DRAG 0x1u  /* a drag value was NaN or Inf */
+#define CLBM_DEV_WEIGHT_OVERFLOW 0x2u /* exp(alpha*s) or the normaliser overflowed */
+#define CLBM_DEV_BAD_DENSITY 0x4u     /* rho <= 0 or NaN at some node */
+#define CLBM_DEV_BAD_PARENT 0x8u      /* resampling produced an invalid parent */
+#define CLBM_DEV_RESAMPLE 0x10u       /* copy numbers could not be corrected */
+#define CLBM_DEV_TIMEOUT 0x20u        /* a bounded spin-wait expired */
+
+/* arithmetic of the populations */
+#define CLBM_FP64 0 /* FP64, reference operation order, no fused multiply-add */
+#define CLBM_FP32 1 /* FP32 populations stored as f - w[k]; FP64 drag integral,
+                       weights, normaliser and SCGF */
+
+/* resampling of the cloning step */
+#define CLBM_RESAMPLE_REFERENCE 0  /* floor(s_j/R + drand48()) + glibc rand()
+                                      kill/duplicate correction, the reference's
+                                      random streams emulated bit for bit */
+#define CLBM_RESAMPLE_SYSTEMATIC 1 /* systematic resampling, one Philox uniform
+                                      per interval, log-domain weights */
+
+/* perturbation of newly created clones (at the start of the next interval) */
+#define CLBM_PERTURB_NONE 0
+#define CLBM_PERTURB_MIX 1     /* snapshot mix, prefactors from drand48 */
+#define CLBM_PERTURB_UNIFORM 2 /* f <- f (1 + eps (2u-1)), u Philox4x32-10 */
+
+/* context creation flags */
+#define CLBM_FLAG_GRAPH 0x1 /* capture each interval in a CUDA graph */
+
+typedef struct {
+  int nx, ny;                 /* Dx, Dy */
+  int xmin, xmax, ymin, ymax; /* square, perimeter nodes inclusive */
+} clbm_geom;
+
+typedef struct {
+  int width, height;          /* Dx, Dy */
+  int xmin, xmax, ymin, ymax; /* square, perimeter nodes inclusive */
+  int nclones;                /* Nc */
+  int ranks;                  /* virtual MPI ranks of the reference's random
+                                 streams (>= 1, divides nclones) */
+  double tau;                 /* BGK relaxation time */
+  double beta;                /* body force beta0 */
+  double alpha;               /* bias k */
+  double force_scale;         /* F <- F*force_scale - force_shift */
+  double force_shift;         /*   (1/F0 and AVG=1.775 under ZERO_MEAN) */
+  double dt;                  /* weight integral: s = dt * sum F */
+  int perturb_mode;           /* CLBM_PERTURB_* */
+  int resample_mode;          /* CLBM_RESAMPLE_* */
+  double eps;                 /* perturbation amplitude */
+  unsigned long long seed;    /* counter-based random streams */
+  int nsnap;                  /* snapshots for CLBM_PERTURB_MIX (<= 64) */
+  int reserved;
+} clbm_run_desc;
+
+typedef struct clbm_ctx clbm_ctx;
+
+const char *clbm_strerror(int status);
+/* last error message of the calling thread (CUDA error text included) */
+const char *clbm_last_error(void);
+int clbm_version(void);
+/* number of CUDA devices visible (0 without a GPU); never fails */
+int clbm_device_count(void);
+
+/* ---- function level: reference functions on one clone, device pointers ---- */
+
+/* streamingAndCollisionComputeMacroBodyForce(fin, fout, rho, ux, uy, beta,
+ * tau), src/lbm_src/streamCollCompute.h:1 / streamCollCompute.cpp:7-48.
+ * fin is overwritten with the post-collision populations; rho/ux/uy may be
+ * NULL. stream is a cudaStream_t (NULL = default stream). */
+int clbm_ref_stream_collide(const clbm_geom *g, double *fin, double *fout,
+                            double *rho, double *ux, double *uy, double beta,
+                            double tau, void *stream);
+/* streamingAndCollisionComputeMacroBodyForceSpatial(fin, fout, rho, ux, uy,
+ * beta0, map, tau, eps), streamCollCompute.h:2 / streamCollCompute.cpp:50-93 */
+int clbm_ref_stream_collide_spatial(const clbm_geom *g, double *fin,
+                                    double *fout, double *rho, double *ux,
+                                    double *uy, double beta0, const double *map,
+                                    double tau, double eps, void *stream);
+/* computeDomainNoSlipWalls_BB(fout, fin), boundaryConditions.h:1 */
+int clbm_ref_walls_bb(const clbm_geom *g, double *fout, const double *fin,
+                      void *stream);
+/* computeSquareBounceBack_TEST(fout, fin), boundaryConditions.h:5 */
+int clbm_ref_square_bb(const clbm_geom *g, double *fout, const double *fin,
+                       void *stream);
+/* interior reset to w[k], src/mpi_LBM_GK_pops_perturb.cpp:430-439 */
+int clbm_ref_interior_reset(const clbm_geom *g, double *fout, void *stream);
+/* computeForceOnSquare(f, omega), src/lbm_src/force.h:1; the result is
+ * written to *result (HOST pointer) after a stream synchronisation. */
+int clbm_ref_force_on_square(const clbm_geom *g, const double *f,
+                             double omega, double *result, void *stream);
+/* generatePerturbedState(fin, snaps, eps, NN, N),
+ * src/perturbation.h:5 / generatePerturbedState.cpp:4-38, with the NN
+ * drand48() prefactors supplied by the caller (HOST array).  snaps is one
+ * DEVICE array of NN*N doubles.  Returns a status (the reference returns an
+ * undefined value). */
+int clbm_ref_perturbed_state(double *fin, const double *snaps, double eps,
+                             int nsnap, int n, const double *prefactors,
+                             void *stream);
+
+/* ---- sampler level ------------------------------------------------------- */
+
+/* max_steps bounds the steps of one interval (drag-term storage). */
+int clbm_create(const clbm_run_desc *runs, int nruns, int precision,
+                int max_steps, int flags, clbm_ctx **out);
+int clbm_destroy(clbm_ctx *ctx);
+
+/* HOST FP64 arrays in the reference AoS layout, N = 9*Dx*Dy values per clone.
+ * Loading replaces the clone's state (reference: the popfiles read at pops
+ * driver :251-310). */
+int clbm_load_pops_aos_f64(clbm_ctx *ctx, int run, int clone,
+                           const double *aos);
+/* all clones of a run at once: aos holds nclones*N values */
+int clbm_load_run_aos_f64(clbm_ctx *ctx, int run, const double *aos);
+/* the clone's current state (after a clone step: its parent's state, before
+ * the pending perturbation) */
+int clbm_dump_pops_aos_f64(clbm_ctx *ctx, int run, int clone, double *aos);
+/* perturbation snapshots of a run, nsnap*N values (pops driver :321-364) */
+int clbm_set_snapshots_aos_f64(clbm_ctx *ctx, int run, int nsnap,
+                               const double *aos);
+/* synthetic initial state of every clone of a run, generated on the device:
+ * equilibrium at rho = 1, u = (u0, 0), times (1 + noise (2u-1)) with a
+ * Philox uniform per population; w[k] inside the square. */
+int clbm_init_equilibrium(clbm_ctx *ctx, int run, double u0, double noise,
+                          unsigned long long seed);
+
+/* one cloning interval of `steps` LB steps for every clone of every run:
+ * pending perturbation of new clones, then per step stream-collide with wall
+ * and square bounce-back and interior reset, the drag on the square after
+ * every step, and the weight integral s_j = dt * sum F (pops driver :399-469). */
+int clbm_run_interval(clbm_ctx *ctx, int steps);
+/* drag series of the last interval, [nclones][steps] F values of a run */
+int clbm_get_drag(clbm_ctx *ctx, int run, double *out);
+/* the cloning step of every run (pops driver :487-701): weights, mean weight
+ * R_t, copy numbers, kill/duplicate correction, copy table, labels; copies
+ * take effect (and new clones are marked for perturbation) for the next
+ * interval. */
+int clbm_clone_step(clbm_ctx *ctx);
+/* results of the last clone step of a run; any pointer may be NULL.
+ * labels[Nc] int32 (parent slot of each slot), *rvalue = R_t,
+ * weights[Nc] = exp(alpha*s_j), copies_pre/post[Nc] int32 copy numbers before
+ * and after the correction (forcing driver :461,:510). */
+int clbm_get_clone_result(clbm_ctx *ctx, int run, int *labels, double *rvalue,
+                          double *weights, int *copies_pre, int *copies_post);
+/* `intervals` x (run_interval + clone_step) without host round trips, as
+ * CUDA graphs when the context was created with CLBM_FLAG_GRAPH.  rvalues
+ * (nullable, [nruns][intervals]) receives R_t of every interval. */
+int clbm_run_sampler(clbm_ctx *ctx, int steps, int intervals, double *rvalues);
+
+/* Timing of the step kernels: while enabled, every interval enqueued
+ * eagerly (run_interval, or run_sampler without CUDA graphs) records a CUDA
+ * event pair around its step launches on the context's stream.  Enabling
+ * resets the accumulators; clbm_profile_read returns the summed milliseconds
+ * and the number of step launches since then (and resets them). */
+int clbm_profile(clbm_ctx *ctx, int enable);
+int clbm_profile_read(clbm_ctx *ctx, double *step_ms, int *nsteps);
+
+/* device error word (CLBM_DEV_* bits) accumulated since the last clear */
+int clbm_error_word(clbm_ctx *ctx, unsigned *word, int clear);
+/* block until the context's stream is idle */
+int clbm_sync(clbm_ctx *ctx);
+/* the context's cudaStream_t */
+void *clbm_stream(clbm_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
