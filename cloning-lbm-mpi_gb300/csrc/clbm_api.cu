@@ -414,8 +414,9 @@ static int check_snapshots(clbm_ctx *c) {
 }
 
 static int sbuf_after(int sbuf, int steps) {
-  // reseed writes P into 1-sbuf, each step flips; the last step writes S
-  return (steps % 2 == 0) ? sbuf : 1 - sbuf;
+  // reseed writes P into 1-sbuf and step t writes into sbuf when t is even,
+  // 1-sbuf when t is odd; the last step (t = steps-1) writes S
+  return (steps % 2 == 1) ? sbuf : 1 - sbuf;
 }
 
 extern "C" int clbm_run_interval(clbm_ctx *c, int steps) {
