@@ -30,7 +30,7 @@ EXPORTS = [
     "clbm_ref_perturbed_state", "clbm_create", "clbm_destroy", "clbm_load_pops_aos_f64",
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
-    "clbm_get_clone_result", "clbm_run_sampler", "clbm_profile", "clbm_profile_read",
+    "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_run_sampler", "clbm_profile", "clbm_profile_read",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -89,6 +89,8 @@ def lib() -> C.CDLL:
         L.clbm_clone_step.argtypes = [vp]
         L.clbm_get_clone_result.argtypes = [vp, i, vp, vp, vp, vp, vp]
         L.clbm_run_sampler.argtypes = [vp, i, i, vp]
+        L.clbm_get_rvalues.argtypes = [vp, i, i, i, vp, vp]
+        L.clbm_intervals_done.argtypes = [vp, i, C.POINTER(i)]
         L.clbm_profile.argtypes = [vp, i]
         L.clbm_profile_read.argtypes = [vp, C.POINTER(d), C.POINTER(i)]
         L.clbm_error_word.argtypes = [vp, C.POINTER(C.c_uint), i]
@@ -232,6 +234,18 @@ class Sampler:
         check(lib().clbm_get_clone_result(self.h, run, _p(labels), C.byref(rv), _p(w), _p(pre), _p(post)),
               "clbm_get_clone_result")
         return {"labels": labels, "rvalue": rv.value, "weights": w, "copies_pre": pre, "copies_post": post}
+
+    def intervals_done(self, run: int = 0) -> int:
+        n = C.c_int()
+        check(lib().clbm_intervals_done(self.h, run, C.byref(n)), "clbm_intervals_done")
+        return n.value
+
+    def rvalues(self, run: int = 0, first: int = 0, count: int | None = None):
+        if count is None:
+            count = self.intervals_done(run) - first
+        rv, lr = np.empty(count), np.empty(count)
+        check(lib().clbm_get_rvalues(self.h, run, first, count, _p(rv), _p(lr)), "clbm_get_rvalues")
+        return rv, lr
 
     def run_sampler(self, steps: int, intervals: int) -> np.ndarray:
         rv = np.empty((len(self.runs), intervals))

@@ -112,7 +112,7 @@ extern "C" int clbm_destroy(clbm_ctx *c) {
   void *bufs[] = {c->pop[0], c->pop[1], c->d.runs, c->d.state, c->d.sacc, c->d.drag, c->d.weights,
                   c->d.labels, c->d.mark, c->d.copies_pre, c->d.copies_post, c->d.prefactors,
                   c->d.pert, c->d.partials, c->d.scratch_i, c->d.scratch_d, c->d.snaps,
-                  c->d.rvalues, c->d.err, c->d.terms, c->d_identity};
+                  c->d.rvalues, c->d.logr, c->d.err, c->d.terms, c->d_identity};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -246,6 +246,7 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
   if ((e = dalloc(D.scratch_d, clones)) != cudaSuccess) return bail(e);
   if ((e = dalloc(D.snaps, (size_t)snaps)) != cudaSuccess) return bail(e);
   if ((e = dalloc(D.rvalues, (size_t)nruns * D.max_intervals)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(D.logr, (size_t)nruns * D.max_intervals)) != cudaSuccess) return bail(e);
   if ((e = dalloc(D.err, 1)) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&D.terms, (size_t)terms * max_steps * c->elem_size)) != cudaSuccess) return bail(e);
   if ((e = dalloc(c->d_identity, clones)) != cudaSuccess) return bail(e);
@@ -456,6 +457,31 @@ extern "C" int clbm_get_drag(clbm_ctx *c, int run, double *out) {
   CK(cudaMemcpy2DAsync(out, sizeof(double) * c->last_steps, c->d.drag + (size_t)R.clone_base * c->max_steps,
                        sizeof(double) * c->max_steps, sizeof(double) * c->last_steps, R.nclones,
                        cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return CLBM_OK;
+}
+
+extern "C" int clbm_get_rvalues(clbm_ctx *c, int run, int first, int count, double *rvalues,
+                                double *log_rvalues) {
+  if (int s = check_run(c, run)) return s;
+  int done = 0;
+  CK(cudaMemcpyAsync(&done, &c->d.state[run].interval, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (first < 0 || count < 0 || first + count > done || first + count > c->d.max_intervals)
+    return fail(CLBM_ERR_INVALID, "requested intervals outside the recorded history");
+  const size_t off = (size_t)run * c->d.max_intervals + first;
+  if (rvalues && count)
+    CK(cudaMemcpyAsync(rvalues, c->d.rvalues + off, sizeof(double) * count, cudaMemcpyDeviceToHost, c->stream));
+  if (log_rvalues && count)
+    CK(cudaMemcpyAsync(log_rvalues, c->d.logr + off, sizeof(double) * count, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return CLBM_OK;
+}
+
+extern "C" int clbm_intervals_done(clbm_ctx *c, int run, int *done) {
+  if (int s = check_run(c, run)) return s;
+  if (!done) return fail(CLBM_ERR_INVALID, "done is NULL");
+  CK(cudaMemcpyAsync(done, &c->d.state[run].interval, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return CLBM_OK;
 }

@@ -99,7 +99,7 @@ __device__ V block_exclusive_scan_total(V v, V *sh, V &total) {
 __global__ void __launch_bounds__(CLONE_THREADS) k_clone(DevArrays d, int nruns) {
   __shared__ int shi[32];
   __shared__ double shd[32];
-  __shared__ double sh_rbar, sh_u, sh_max;
+  __shared__ double sh_rbar, sh_logr, sh_u, sh_max;
   __shared__ int sh_status;
   const int r = blockIdx.x;
   const RunDev &R = d.runs[r];
@@ -113,7 +113,11 @@ __global__ void __launch_bounds__(CLONE_THREADS) k_clone(DevArrays d, int nruns)
   int *extras = temp + 2 * nc + 2;               // nc surplus copies' parents
   double *pre = d.scratch_d + g0;                // nc prefix sums
   const bool systematic = R.resample_mode == 1;
-  if (threadIdx.x == 0) sh_status = 0;
+  if (threadIdx.x == 0) {
+    sh_status = 0;
+    sh_rbar = NAN;
+    sh_logr = NAN;
+  }
 
   // ---- weights (pops driver :465-469) ----
   double locmax = -INFINITY;
@@ -138,6 +142,7 @@ __global__ void __launch_bounds__(CLONE_THREADS) k_clone(DevArrays d, int nruns)
       }
       const double rbar = DDIV(total, (double)nc);
       sh_rbar = rbar;
+      sh_logr = log(rbar);
       if (!isfinite(rbar) || !(rbar > 0.0)) sh_status = ERR_WEIGHT_OVERFLOW;
     }
     __syncthreads();
@@ -178,7 +183,10 @@ __global__ void __launch_bounds__(CLONE_THREADS) k_clone(DevArrays d, int nruns)
     double tot;
     const double off = block_exclusive_scan_total<double>(acc, shd, tot);
     for (int j = j0; j < j1; j++) pre[j] = DADD(pre[j], off);
-    if (threadIdx.x == 0) sh_rbar = DMUL(exp(sh_max), DDIV(tot, (double)nc));
+    if (threadIdx.x == 0) {
+      sh_logr = DADD(sh_max, log(DDIV(tot, (double)nc)));
+      sh_rbar = exp(sh_logr);
+    }
     __syncthreads();
     const double last = pre[nc - 1];
     for (int j = j0; j < j1; j++) {
@@ -286,7 +294,11 @@ __global__ void __launch_bounds__(CLONE_THREADS) k_clone(DevArrays d, int nruns)
     if (threadIdx.x == 0) {
       st.ncomm = killed;
       st.rbar = sh_rbar;
-      if (st.interval < d.max_intervals) d.rvalues[(long long)r * d.max_intervals + st.interval] = sh_rbar;
+      st.logr = sh_logr;
+      if (st.interval < d.max_intervals) {
+        d.rvalues[(long long)r * d.max_intervals + st.interval] = sh_rbar;
+        d.logr[(long long)r * d.max_intervals + st.interval] = sh_logr;
+      }
       st.interval += 1;
     }
     return;
@@ -301,6 +313,7 @@ fail:
   if (threadIdx.x == 0) {
     atomicOr(d.err, (unsigned)sh_status);
     st.rbar = sh_rbar;
+    st.logr = sh_logr;
     st.interval += 1;
   }
 }

@@ -22,6 +22,7 @@ struct RunState {
   int ncopies_drawn;                  // NcPrime of the last clone step
   int pad_;
   double rbar;                        // R_t of the last clone step
+  double logr;                        // log R_t (finite where R_t overflows)
 };
 
 // Device arrays of one context (all indexed by global clone index unless
@@ -43,6 +44,7 @@ struct DevArrays {
   double *scratch_d;  // per run: nclones doubles (prefix sums)
   double *snaps;      // per run: nsnap * 9 * plane FP64, SoA like the populations
   double *rvalues;    // per run: [max_intervals] R_t history
+  double *logr;       // per run: [max_intervals] log R_t history
   unsigned *err;      // device error word
   void *terms;        // [max_steps][slab] drag terms (double or float)
   long long term_slab;// terms per step over all runs

@@ -185,6 +185,13 @@ int clbm_clone_step(clbm_ctx *ctx);
  * and after the correction (forcing driver :461,:510). */
 int clbm_get_clone_result(clbm_ctx *ctx, int run, int *labels, double *rvalue,
                           double *weights, int *copies_pre, int *copies_post);
+/* R_t and log R_t of intervals [first, first+count) of a run (history of up
+ * to 65536 cloning steps; log R_t stays finite where R_t overflows, e.g.
+ * under systematic resampling at a large bias).  Either pointer may be NULL. */
+int clbm_get_rvalues(clbm_ctx *ctx, int run, int first, int count,
+                     double *rvalues, double *log_rvalues);
+/* number of cloning steps a run has completed */
+int clbm_intervals_done(clbm_ctx *ctx, int run, int *done);
 /* `intervals` x (run_interval + clone_step) without host round trips, as
  * CUDA graphs when the context was created with CLBM_FLAG_GRAPH.  rvalues
  * (nullable, [nruns][intervals]) receives R_t of every interval. */

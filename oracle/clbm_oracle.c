@@ -421,7 +421,7 @@ orc_clone_result orc_clone_reference(int nc, int ranks, const double *s,
                                      orc_drand48 *master, orc_glibc_rand *rnd,
                                      int *copies_pre, int *copies_post,
                                      int *labels, int *table) {
-  orc_clone_result res = {0.0, 0, 0, 0};
+  orc_clone_result res = {0.0, 0.0, 0, 0, 0};
   const int local = nc / ranks;
   double total = 0.0;
   for (int r = 0; r < ranks; r++) {
@@ -434,6 +434,7 @@ orc_clone_result orc_clone_reference(int nc, int ranks, const double *s,
   }
   total /= nc;
   res.rbar = total;
+  res.logr = log(total);
   if (!isfinite(total) || !(total > 0.0)) {
     res.status = -3;
     return res;
@@ -491,7 +492,7 @@ orc_clone_result orc_clone_reference(int nc, int ranks, const double *s,
  * n_j = floor(c_j + u) - floor(c_{j-1} + u), which sums to Nc exactly. */
 orc_clone_result orc_clone_systematic(int nc, const double *logw, double u,
                                       int *copies, int *labels, int *table) {
-  orc_clone_result res = {0.0, 0, 0, 0};
+  orc_clone_result res = {0.0, 0.0, 0, 0, 0};
   double m = -INFINITY;
   for (int j = 0; j < nc; j++)
     if (logw[j] > m) m = logw[j];
@@ -502,7 +503,8 @@ orc_clone_result orc_clone_systematic(int nc, const double *logw, double u,
     acc += exp(logw[j] - m);
     p[j] = acc;
   }
-  res.rbar = exp(m) * (acc / nc);
+  res.logr = m + log(acc / nc);
+  res.rbar = exp(res.logr);
   double prev = floor(u);
   for (int j = 0; j < nc; j++) {
     double c = (p[j] / acc) * nc;
@@ -526,10 +528,12 @@ orc_clone_result orc_clone_systematic(int nc, const double *logw, double u,
  * numbers and the glibc rand() corrections (srand(1) + 1000 discards).  New
  * clones are perturbed at the start of the next interval (_SMART_PERTURB).
  * Outputs (all optional): drag[t][j][tt] = F/F0 - shift, labels[t][j],
- * rvalues[t], weights[t][j] = exp(alpha s_j), copies[t][2][j]. */
+ * rvalues[t], logr[t] = log R_t, weights[t][j] = exp(alpha s_j),
+ * copies[t][2][j]. */
 int orc_run_sampler(const orc_sampler_cfg *cfg, double *states,
                     const double *snaps, double *drag, int *labels,
-                    double *rvalues, double *weights, int *copies) {
+                    double *rvalues, double *logr, double *weights,
+                    int *copies) {
   const orc_geom *g = &cfg->g;
   const int nc = cfg->nclones;
   const int n = 9 * g->nx * g->ny;
@@ -602,6 +606,7 @@ int orc_run_sampler(const orc_sampler_cfg *cfg, double *states,
       break;
     }
     if (rvalues) rvalues[t] = cr.rbar;
+    if (logr) logr[t] = cr.logr;
     if (labels) memcpy(labels + (size_t)t * nc, lab, sizeof(int) * nc);
     if (copies) {
       memcpy(copies + (size_t)t * 2 * nc, pre, sizeof(int) * nc);

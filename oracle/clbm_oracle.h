@@ -73,6 +73,7 @@ void orc_init_equilibrium(double *fin, const orc_geom *g, double u0,
 /* ---- cloning step (src/mpi_LBM_GK_pops_perturb.cpp:487-624) ------------------ */
 typedef struct {
   double rbar;      /* R_t, the normalised mean weight */
+  double logr;      /* log R_t (finite where R_t itself overflows) */
   int ncopies_drawn;/* NcPrime */
   int ncomm;        /* number of clone copies */
   int status;       /* 0 ok, <0 error */
@@ -98,7 +99,8 @@ typedef struct {
 } orc_sampler_cfg;
 int orc_run_sampler(const orc_sampler_cfg *cfg, double *states,
                     const double *snaps, double *drag, int *labels,
-                    double *rvalues, double *weights, int *copies);
+                    double *rvalues, double *logr, double *weights,
+                    int *copies);
 
 /* ---- CPU baseline timing: nclones independent clones, nthreads threads ---- */
 double orc_bench_lbm(const orc_geom *g, int nclones, int steps, double tau,

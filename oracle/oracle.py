@@ -51,8 +51,8 @@ class GlibcRand(C.Structure):
 
 
 class CloneResult(C.Structure):
-    _fields_ = [("rbar", C.c_double), ("ncopies_drawn", C.c_int), ("ncomm", C.c_int),
-                ("status", C.c_int)]
+    _fields_ = [("rbar", C.c_double), ("logr", C.c_double), ("ncopies_drawn", C.c_int),
+                ("ncomm", C.c_int), ("status", C.c_int)]
 
 
 def build() -> Path:
@@ -220,13 +220,14 @@ def run_sampler(g: Geom, states: np.ndarray, *, steps: int, intervals: int, tau:
     drag = np.zeros((intervals, nc, steps))
     labels = np.zeros((intervals, nc), np.int32)
     rv = np.zeros(intervals)
+    logr = np.zeros(intervals)
     wts = np.zeros((intervals, nc))
     cop = np.zeros((intervals, 2, nc), np.int32)
     sn = None if snaps is None else np.ascontiguousarray(snaps, dtype=np.float64)
     status = lib().orc_run_sampler(C.byref(cfg), _p(st), _p(sn), _p(drag), _p(labels), _p(rv),
-                                   _p(wts), _p(cop))
+                                   _p(logr), _p(wts), _p(cop))
     return {"status": status, "states": st, "drag": drag, "labels": labels, "rvalues": rv,
-            "weights": wts, "copies": cop}
+            "logr": logr, "weights": wts, "copies": cop}
 
 
 def bench_lbm(g: Geom, nclones: int, steps: int, tau: float, beta: float, nthreads: int) -> tuple[float, float]:

@@ -51,7 +51,9 @@ def test_pops_driver_golden(gpu, clbm_lib, orc, i):
             rv.append(r["rvalue"])
     force = np.concatenate(force, axis=1)
     assert np.array_equal(np.concatenate(labels), z[f"run{i}_labels"])
-    np.testing.assert_allclose(rv, z[f"run{i}_rvalues"], rtol=1e-13)
+    # R_t = mean exp(alpha s): alpha (up to 20 here) amplifies the ulp-level
+    # rounding of the tree-ordered perturbation norms
+    np.testing.assert_allclose(rv, z[f"run{i}_rvalues"], rtol=1e-11)
     assert rel(force, z[f"run{i}_force"]) < 1e-12
     # before the first perturbation the series is bit-identical
     assert np.array_equal(force[:, :sc["steps"]], z[f"run{i}_force"][:, :sc["steps"]])
@@ -64,9 +66,9 @@ def channel_case(orc, W=64, H=24, side=6, nc=8, u0=0.05, tau=0.56, k=2.0, T=40, 
     return g, dict(tau=tau, beta=beta, alpha=k, force_scale=1 / F0, force_shift=0.0, dt=u0 / side), T, n, nc, seed
 
 
-@pytest.mark.parametrize("resample", [0, 1])
-def test_fp64_uniform_perturbation_matches_oracle(gpu, clbm_lib, orc, resample):
-    g, phys, T, n, nc, seed = channel_case(orc)
+@pytest.mark.parametrize("resample,k", [(0, 2.0), (1, 100.0)])
+def test_fp64_uniform_perturbation_matches_oracle(gpu, clbm_lib, orc, resample, k):
+    g, phys, T, n, nc, seed = channel_case(orc, k=k)
     states = np.concatenate([orc.init_equilibrium(g, 0.05, 1e-3, seed, 0, j) for j in range(nc)])
     ref = orc.run_sampler(g, states, steps=T, intervals=n, perturb_mode=2, resample_mode=resample,
                           eps=1e-4, seed=seed, **phys)
@@ -84,6 +86,8 @@ def test_fp64_uniform_perturbation_matches_oracle(gpu, clbm_lib, orc, resample):
             assert np.array_equal(r["labels"], ref["labels"][t])
             np.testing.assert_allclose(r["rvalue"], ref["rvalues"][t], rtol=1e-14)
         assert (ref["labels"] != np.arange(nc)).any()
+        rv, lr = s.rvalues(0)
+        np.testing.assert_allclose(lr, ref["logr"], rtol=1e-14, atol=1e-14)
         for j in range(nc):
             np.testing.assert_array_equal(s.dump(0, j), ref["states"][j * 9 * g.nx * g.ny:(j + 1) * 9 * g.nx * g.ny])
 
@@ -168,7 +172,8 @@ def test_fp32_against_fp64_oracle(gpu, clbm_lib, orc):
         err = rel(s.drag(0), ref["drag"][0])
         assert err < 1e-5, err
         s.clone_step()
-        np.testing.assert_allclose(s.clone_result(0)["weights"], ref["weights"][0], rtol=1e-6)
+        # weights exp(alpha s): relative error about alpha * s * (drag error)
+        np.testing.assert_allclose(s.clone_result(0)["weights"], ref["weights"][0], rtol=2e-4)
 
 
 def test_weight_overflow_is_reported(gpu, clbm_lib, orc):
