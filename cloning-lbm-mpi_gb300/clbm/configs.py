@@ -106,4 +106,15 @@ def c4() -> Workload:
     return Workload("c4_uneven_8x256", runs, 100, 40, FP32)
 
 
-WORKLOADS = {"c1": c1, "c2": c2, "c3": c3, "c4": c4}
+def c3_small() -> Workload:
+    """256 clones of the c3 lattice (151 MB per FP32 buffer, above L2): the
+    case the ncu captures of the step kernel run on."""
+    return Workload("c3s_256x256x64_fp32",
+                    [Run(256, 64, 12, 64, 32, 256, 0.04, 0.55, 0.3, 1e-5, 3)], 100, 100, FP32)
+
+
+def c2_fp32() -> Workload:
+    return c2(FP32)
+
+
+WORKLOADS = {"c1": c1, "c2": c2, "c2f32": c2_fp32, "c3": c3, "c3s": c3_small, "c4": c4}
