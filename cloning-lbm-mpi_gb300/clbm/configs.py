@@ -113,8 +113,15 @@ def c3_small() -> Workload:
                     [Run(256, 64, 12, 64, 32, 256, 0.04, 0.55, 0.3, 1e-5, 3)], 100, 100, FP32)
 
 
+def c3_medium() -> Workload:
+    """1024 clones of the c3 lattice (604 MB per FP32 buffer, 4.7x L2): the
+    case the DRAM-traffic capture of the step kernel runs on."""
+    return Workload("c3m_1024x256x64_fp32",
+                    [Run(256, 64, 12, 64, 32, 1024, 0.04, 0.55, 0.3, 1e-5, 3)], 100, 100, FP32)
+
+
 def c2_fp32() -> Workload:
     return c2(FP32)
 
 
-WORKLOADS = {"c1": c1, "c2": c2, "c2f32": c2_fp32, "c3": c3, "c3s": c3_small, "c4": c4}
+WORKLOADS = {"c1": c1, "c2": c2, "c2f32": c2_fp32, "c3": c3, "c3s": c3_small, "c3m": c3_medium, "c4": c4}
