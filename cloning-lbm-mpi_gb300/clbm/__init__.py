@@ -27,7 +27,7 @@ EXPORTS = [
     "clbm_strerror", "clbm_last_error", "clbm_version", "clbm_device_count",
     "clbm_ref_stream_collide", "clbm_ref_stream_collide_spatial", "clbm_ref_walls_bb",
     "clbm_ref_square_bb", "clbm_ref_interior_reset", "clbm_ref_force_on_square",
-    "clbm_ref_perturbed_state", "clbm_create", "clbm_destroy", "clbm_load_pops_aos_f64",
+    "clbm_ref_perturbed_state", "clbm_ref_perturbed_state_noalloc", "clbm_create", "clbm_destroy", "clbm_load_pops_aos_f64",
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_run_sampler", "clbm_profile", "clbm_profile_read",
@@ -77,6 +77,7 @@ def lib() -> C.CDLL:
         L.clbm_ref_interior_reset.argtypes = [C.POINTER(Geom), vp, vp]
         L.clbm_ref_force_on_square.argtypes = [C.POINTER(Geom), vp, d, C.POINTER(d), vp]
         L.clbm_ref_perturbed_state.argtypes = [vp, vp, d, i, i, vp, vp]
+        L.clbm_ref_perturbed_state_noalloc.argtypes = [vp, vp, d, i, i, vp, vp]
         L.clbm_create.argtypes = [C.POINTER(RunDesc), i, i, i, i, C.POINTER(vp)]
         L.clbm_destroy.argtypes = [vp]
         L.clbm_load_pops_aos_f64.argtypes = [vp, i, i, vp]
@@ -152,6 +153,12 @@ def ref_perturbed_state(fin, snaps, eps, nsnap, n, prefactors: np.ndarray, strea
     pre = np.ascontiguousarray(prefactors, dtype=np.float64)
     check(lib().clbm_ref_perturbed_state(fin, snaps, eps, nsnap, n, _p(pre), stream),
           "clbm_ref_perturbed_state")
+
+
+def ref_perturbed_state_noalloc(fin, snaps, eps, nsnap, n, prefactors: np.ndarray, stream=None):
+    pre = np.ascontiguousarray(prefactors, dtype=np.float64)
+    check(lib().clbm_ref_perturbed_state_noalloc(fin, snaps, eps, nsnap, n, _p(pre), stream),
+          "clbm_ref_perturbed_state_noalloc")
 
 
 # ---- sampler level ----

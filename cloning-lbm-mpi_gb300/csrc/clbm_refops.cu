@@ -3,6 +3,7 @@
 // IDX(x,y,k) = k + 9*(y + Dy*x) (src/lbm_src/global.h:4), on device pointers,
 // with the reference's operation order (bit-identical results).
 #include <cstdio>
+#include <mutex>
 
 #include "../../include/clbm.h"
 #include "clbm_physics.cuh"
@@ -297,6 +298,77 @@ extern "C" int clbm_ref_perturbed_state(double *fin, const double *snaps, double
     e = cudaGetLastError();
   }
   cudaFreeAsync(d_buf, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return clbm_status_from_cuda(e);
+}
+
+// ---------------------------------------------------------------------------
+// clbm_ref_perturbed_state_noalloc: the same two kernels as
+// clbm_ref_perturbed_state, with their scratch (the snapshot prefactors and
+// two norm partial sums per 256 values) in a fixed device array instead of a
+// per-call allocation.  It serves callers that must not allocate device
+// memory at all: code running under an allocator that already owns the whole
+// device, or inside a time-critical loop where an allocation's implicit
+// synchronisation is not acceptable.
+namespace {
+constexpr int NOALLOC_MAX_N = 1 << 20;                     // values per state, 9*Dx*Dy
+constexpr int NOALLOC_MAX_BLOCKS = NOALLOC_MAX_N / 256;    // norm partials (pairs)
+constexpr int NOALLOC_PREF = 64;                           // prefactor slots (nsnap <= 64)
+// Shared by every call on a device and kept until the process exits
+// (66 KB per device that loads the library).  Nothing in it has to start at
+// zero: each call overwrites the prefactors and every partial it reads.
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_PREF + 2 * NOALLOC_MAX_BLOCKS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+double *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+// The array's device address on the current device, looked up once per
+// device with that device current (the host-side symbol is not a device
+// address and must never be passed to a kernel).
+int noalloc_scratch(double **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return clbm_status_from_cuda(e);
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+    clbm_set_error("device ordinal beyond the no-alloc scratch table");
+    return CLBM_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    double *p = nullptr;
+    e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return clbm_status_from_cuda(e);
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return CLBM_OK;
+}
+}  // namespace
+
+extern "C" int clbm_ref_perturbed_state_noalloc(double *fin, const double *snaps, double eps,
+                                                int nsnap, int n, const double *prefactors,
+                                                void *stream) {
+  if (!fin || !snaps || !prefactors || nsnap < 1 || nsnap > NOALLOC_PREF || n < 1) {
+    clbm_set_error("invalid argument");
+    return CLBM_ERR_INVALID;
+  }
+  if (n > NOALLOC_MAX_N) {
+    clbm_set_error("n exceeds the no-alloc scratch limit of 1048576 values (9*Dx*Dy)");
+    return CLBM_ERR_INVALID;
+  }
+  double *scratch = nullptr;
+  if (int s = noalloc_scratch(&scratch)) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nb = (n + 255) / 256;
+  double *d_pref = scratch, *d_part = scratch + NOALLOC_PREF;
+  cudaError_t e = cudaMemcpyAsync(d_pref, prefactors, sizeof(double) * nsnap,
+                                  cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    k_ref_perturb_norms<<<nb, 256, 0, st>>>(fin, snaps, nsnap, n, d_pref, d_part);
+    k_ref_perturb_apply<<<nb, 256, 0, st>>>(fin, snaps, nsnap, n, d_pref, d_part, nb, eps);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return clbm_status_from_cuda(e);
 }

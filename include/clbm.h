@@ -140,6 +140,20 @@ int clbm_ref_force_on_square(const clbm_geom *g, const double *f,
 int clbm_ref_perturbed_state(double *fin, const double *snaps, double eps,
                              int nsnap, int n, const double *prefactors,
                              void *stream);
+/* Same computation and result as clbm_ref_perturbed_state, for callers that
+ * cannot allocate device memory (an allocator owns the whole device, or an
+ * allocation's implicit synchronisation is not allowed in their loop).  No
+ * counterpart in the reference.  It allocates nothing: its scratch (the
+ * prefactors and the per-block norm partials) lives in one fixed device array
+ * of 66 KB that every GPU loading the library holds until exit, so n (the
+ * values of one state, 9*Dx*Dy) is limited to 1048576 and nsnap to 64; larger
+ * sizes return CLBM_ERR_INVALID.  The first call on a device looks up the
+ * array's device address, so make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller. */
+int clbm_ref_perturbed_state_noalloc(double *fin, const double *snaps,
+                                     double eps, int nsnap, int n,
+                                     const double *prefactors, void *stream);
 
 /* ---- sampler level ------------------------------------------------------- */
 
