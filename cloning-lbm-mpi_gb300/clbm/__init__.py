@@ -30,7 +30,7 @@ EXPORTS = [
     "clbm_ref_perturbed_state", "clbm_ref_perturbed_state_noalloc", "clbm_create", "clbm_destroy", "clbm_load_pops_aos_f64",
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
-    "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_run_sampler", "clbm_profile", "clbm_profile_read",
+    "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -93,6 +93,8 @@ def lib() -> C.CDLL:
         L.clbm_get_rvalues.argtypes = [vp, i, i, i, vp, vp]
         L.clbm_intervals_done.argtypes = [vp, i, C.POINTER(i)]
         L.clbm_profile.argtypes = [vp, i]
+        L.clbm_autotune.argtypes = [vp, i, C.POINTER(i), vp, C.POINTER(i)]
+        L.clbm_set_step_variant.argtypes = [vp, i]
         L.clbm_profile_read.argtypes = [vp, C.POINTER(d), C.POINTER(i)]
         L.clbm_error_word.argtypes = [vp, C.POINTER(C.c_uint), i]
         L.clbm_sync.argtypes = [vp]
@@ -259,6 +261,17 @@ class Sampler:
         check(lib().clbm_run_sampler(self.h, steps, intervals, _p(rv)), "clbm_run_sampler")
         self.last_steps = steps
         return rv
+
+    def autotune(self, launches: int = 5, measure: bool = True):
+        """Returns (best variant, ms per launch of every variant)."""
+        best, nv = C.c_int(), C.c_int()
+        ms = np.zeros(32)
+        check(lib().clbm_autotune(self.h, launches, C.byref(best), _p(ms) if measure else None,
+                                  C.byref(nv)), "clbm_autotune")
+        return best.value, ms[:nv.value]
+
+    def set_step_variant(self, v: int):
+        check(lib().clbm_set_step_variant(self.h, v), "clbm_set_step_variant")
 
     def profile(self, enable: bool):
         check(lib().clbm_profile(self.h, int(enable)), "clbm_profile")

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/clbm.h"
@@ -64,6 +65,8 @@ struct clbm_ctx {
   std::vector<cudaEvent_t> ev;  // 2 per profiled interval
   int ev_used = 0;
   int prof_steps = 0;
+  int max_nodes = 0;
+  int step_variant = 0;  // FP32 step launch variant (clbm_autotune)
 };
 
 extern "C" const char *clbm_strerror(int status) {
@@ -212,6 +215,11 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
     }
     clones += d.nclones;
     blocks += d.nclones * R.blocks_per_clone;
+    c->max_nodes = std::max(c->max_nodes, R.nodes);
+  }
+  if (clones > 65535) {
+    delete c;
+    return fail(CLBM_ERR_INVALID, "more than 65535 clones in one context");
   }
   c->total_clones = clones;
   c->total_blocks = blocks;
@@ -394,8 +402,10 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
     if ((e = cudaEventRecord(e0, s)) != cudaSuccess) return e;
   }
   for (int t = 0; t < steps; t++) {
-    StepArgs a{c->d.runs, c->nruns, t, c->pop[cur], c->pop[1 - cur], c->d.terms, c->d.term_slab, c->d.err};
-    if ((e = launch_step(f64, t == steps - 1, a, c->total_blocks, s)) != cudaSuccess) return e;
+    StepArgs a{c->d.runs, c->nruns, t, c->pop[cur], c->pop[1 - cur], c->d.terms, c->d.term_slab,
+               c->d.err, c->total_clones, c->max_nodes};
+    if ((e = launch_step(f64, t == steps - 1, a, c->total_blocks, s, c->step_variant)) != cudaSuccess)
+      return e;
     cur = 1 - cur;
   }
   if (prof && (e = cudaEventRecord(e1, s)) != cudaSuccess) return e;
@@ -607,5 +617,88 @@ extern "C" int clbm_profile_read(clbm_ctx *c, double *step_ms, int *nsteps) {
   *nsteps = c->prof_steps;
   c->ev_used = 0;
   c->prof_steps = 0;
+  return CLBM_OK;
+}
+
+// Autotuner: time every FP32 step variant on this context's own workload and
+// keep the fastest.  It runs at an interval boundary, reading the current
+// state and writing the idle buffer (overwritten by the next interval's first
+// kernel), so the sampler's state is untouched.  Results are cached per
+// (lattice sizes, clone counts) for the process.
+#include <map>
+#include <mutex>
+static std::mutex g_tune_mutex;
+static std::map<std::vector<long long>, int> g_tune_cache;
+
+extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_per_variant,
+                             int *nvariants) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  const int nv = step_variant_count();
+  if (nvariants) *nvariants = nv;
+  if (c->precision != CLBM_FP32) {
+    if (best) *best = 0;
+    return CLBM_OK;
+  }
+  std::vector<long long> key;
+  for (const RunDev &R : c->runs_h) {
+    key.push_back(R.W);
+    key.push_back(R.H);
+    key.push_back(R.nclones);
+  }
+  if (!ms_per_variant) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      c->step_variant = it->second;
+      if (best) *best = it->second;
+      return CLBM_OK;
+    }
+  }
+  if (launches < 1) launches = 5;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int arg = 0;
+  double best_ms = 1e30;
+  for (int v = 0; v < nv; v++) {
+    StepArgs a{c->d.runs, c->nruns, 0, c->pop[c->s_buf], c->pop[1 - c->s_buf], c->d.terms,
+               c->d.term_slab, c->d.err, c->total_clones, c->max_nodes};
+    cudaError_t e = launch_step(false, false, a, c->total_blocks, c->stream, v);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+    for (int i = 0; i < launches && e == cudaSuccess; i++)
+      e = launch_step(false, false, a, c->total_blocks, c->stream, v);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return clbm_status_from_cuda(e);
+    }
+    const double per = ms / launches;
+    if (ms_per_variant) ms_per_variant[v] = per;
+    if (per < best_ms) {
+      best_ms = per;
+      arg = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->step_variant = arg;
+  destroy_graphs(c);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = arg;
+  }
+  if (best) *best = arg;
+  return CLBM_OK;
+}
+
+extern "C" int clbm_set_step_variant(clbm_ctx *c, int variant) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  if (variant < 0 || variant >= step_variant_count()) return fail(CLBM_ERR_INVALID, "no such variant");
+  c->step_variant = variant;
+  destroy_graphs(c);
   return CLBM_OK;
 }

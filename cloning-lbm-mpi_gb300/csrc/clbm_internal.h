@@ -61,6 +61,8 @@ struct StepArgs {
   void *terms;        // base of the term slabs
   long long term_slab;
   unsigned *err;
+  int total_clones;   // grid y of the FP32 step
+  int max_nodes;      // largest W*H of the runs (grid x = tiles of it)
 };
 
 struct ReseedArgs {
@@ -78,7 +80,10 @@ struct ReseedArgs {
 };
 
 // kernel launchers (clbm_step.cu, clbm_cloning.cu)
-cudaError_t launch_step(bool f64, bool last, const StepArgs &a, int blocks, cudaStream_t s);
+cudaError_t launch_step(bool f64, bool last, const StepArgs &a, int blocks, cudaStream_t s,
+                        int variant);
+int step_variant_count();
+int step_variant_block(int variant);
 cudaError_t launch_reseed(bool f64, const ReseedArgs &a, int blocks, cudaStream_t s);
 cudaError_t launch_perturb_norms(bool f64, const RunDev *runs, int nruns, const void *src,
                                  const int *labels, const int *mark, const double *prefactors,

@@ -140,6 +140,64 @@ __device__ __forceinline__ void collide_f32(const float g[9], float out[9], floa
   }
 }
 
+// The same collision organised by opposite pairs (k, opp k): they share
+// |c.u|, so with e = c_k.u the equilibria split into an even part
+// w (drho + rho (4.5 e^2 - 1.5 u^2)) and an odd part +-3 w rho e, and the
+// Guo terms into w fb (9 cx e - 3 ux) and +-3 w fb cx.  Returns drho.
+__device__ __forceinline__ float collide_f32_pairs(const float g[9], float out[9], float beta,
+                                                   float omega, float cforce) {
+  const float drho = ((g[0] + (g[1] + g[3])) + (g[2] + g[4])) + ((g[5] + g[7]) + (g[6] + g[8]));
+  const float jx = (g[1] - g[3]) + ((g[5] - g[7]) + (g[8] - g[6]));
+  const float jy = (g[2] - g[4]) + ((g[5] - g[7]) + (g[6] - g[8]));
+  const float rho = 1.0f + drho;
+  const float inv = __frcp_rn(rho);
+  const float ux = (jx + 0.5f * beta) * inv;
+  const float uy = jy * inv;
+  const float u2 = 1.5f * (ux * ux + uy * uy);
+  const float fb = cforce * beta;
+  const float om1 = 1.0f - omega;
+  const float base = drho - rho * u2;      // even part before the e^2 term (per unit weight)
+  const float fx = -3.0f * fb * ux;        // Guo even part for cx = 0 (per unit weight)
+  // k = 0
+  out[0] = om1 * g[0] + (4.0f / 9.0f) * (omega * base + fx);
+  const float r45 = 4.5f * rho, r3 = 3.0f * rho;
+  // axis pairs (1,3): e = ux, cx = 1; (2,4): e = uy, cx = 0
+  {
+    const float w = 1.0f / 9.0f;
+    const float e = ux;
+    const float ev = w * (omega * (base + r45 * e * e) + (9.0f * fb * e + fx));
+    const float od = w * (omega * r3 * e + 3.0f * fb);
+    out[1] = om1 * g[1] + (ev + od);
+    out[3] = om1 * g[3] + (ev - od);
+  }
+  {
+    const float w = 1.0f / 9.0f;
+    const float e = uy;
+    const float ev = w * (omega * (base + r45 * e * e) + fx);
+    const float od = w * (omega * r3 * e);
+    out[2] = om1 * g[2] + (ev + od);
+    out[4] = om1 * g[4] + (ev - od);
+  }
+  // diagonal pairs (5,7): e = ux + uy, cx = 1; (6,8): e = uy - ux, cx = -1
+  {
+    const float w = 1.0f / 36.0f;
+    const float e = ux + uy;
+    const float ev = w * (omega * (base + r45 * e * e) + (9.0f * fb * e + fx));
+    const float od = w * (omega * r3 * e + 3.0f * fb);
+    out[5] = om1 * g[5] + (ev + od);
+    out[7] = om1 * g[7] + (ev - od);
+  }
+  {
+    const float w = 1.0f / 36.0f;
+    const float e = uy - ux;
+    const float ev = w * (omega * (base + r45 * e * e) + (-9.0f * fb * e + fx));
+    const float od = w * (omega * r3 * e - 3.0f * fb);
+    out[6] = om1 * g[6] + (ev + od);
+    out[8] = om1 * g[8] + (ev - od);
+  }
+  return drho;
+}
+
 // Drag terms from shifted populations, rest parts removed analytically:
 //   pi_xx = sum_{cx!=0} g - drho/3 - rho ux^2,  pi_xy = g5 - g6 + g7 - g8 - rho ux uy
 // and the West/East rho/3 becomes drho/3 (the +-1/3 cancel between sides).

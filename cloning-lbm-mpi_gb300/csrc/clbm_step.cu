@@ -160,17 +160,117 @@ __global__ void __launch_bounds__(STEP_BLOCK) k_step(StepArgs a) {
   }
 }
 
-cudaError_t launch_step(bool f64, bool last, const StepArgs &a, int blocks, cudaStream_t s) {
+// ---------------------------------------------------------------------------
+// FP32 step, the hot kernel.  Grid: x = tile of BLOCK consecutive nodes,
+// y = global clone index (no integer division to find the work).  Warps with
+// no node on a wall row or in the square's bounding box (the bulk) take a
+// path without any bounce-back selects; the decision is warp-uniform.
+// Collision by opposite pairs (collide_f32_pairs).
+template <int BLOCK, int MINB, bool CS, bool LAST>
+__global__ void __launch_bounds__(BLOCK, MINB) k_step_f32(StepArgs a) {
+  const int gclone = blockIdx.y;
+  int r = 0;
+  while (r + 1 < a.nruns && gclone >= a.runs[r + 1].clone_base) r++;
+  const RunDev &R = a.runs[r];
+  const int clone = gclone - R.clone_base;
+  const int n = blockIdx.x * BLOCK + threadIdx.x;
+  const int W = R.W, H = R.H;
+  const bool valid = n < R.nodes;
+  const int y = (int)__umulhi((unsigned)n, R.div_w);
+  const int x = n - y * W;
+  const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+  const bool near = valid && (in_box || y == 0 || y == H - 1);
+  const bool warp_near = __any_sync(0xffffffffu, near);
+  if (!valid) return;
+  const int plane = (int)R.plane;
+  const long long cb = R.pop_base + (long long)clone * 9 * R.plane;
+  const float *__restrict__ src = (const float *)a.src + cb;
+  float *__restrict__ dst = (float *)a.dst + cb;
+  const int xl = (x == 0) ? W - 1 : x - 1;
+  const int xr = (x == W - 1) ? 0 : x + 1;
+  const int row = y * W;
+  int off[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const int cx = cx_of(k), cy = cy_of(k);
+    const int sx = cx == 1 ? xl : (cx == -1 ? xr : x);
+    const int srow = cy == 1 ? row - W : (cy == -1 ? row + W : row);
+    off[k] = k * plane + srow + sx;
+  }
+  if (warp_near) {
+    const int mask = near ? bounce_mask(R, x, y) : 0;
+    if (mask & 512) {
+      if (LAST) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) dst[k * plane + n] = 0.0f;
+      }
+      return;
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      if ((mask >> k) & 1) off[k] = opp_of(k) * plane + n;
+  }
+  float S[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) S[k] = __ldg(src + off[k]);
+  if (in_box) {
+    float *terms = (float *)a.terms + (long long)a.step * a.term_slab + R.term_base;
+    store_drag_terms<false>(R, S, x, y, clone, terms);
+  }
+  float P[9];
+  float drho;
+  if (LAST) {
+    drho = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      P[k] = S[k];
+      drho += S[k];
+    }
+  } else {
+    drho = collide_f32_pairs(S, P, R.f_beta, R.f_omega, R.f_cforce);
+  }
+  if (!(drho > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    if (CS)
+      __stcs(dst + k * plane + n, P[k]);
+    else
+      dst[k * plane + n] = P[k];
+  }
+}
+
+struct F32Variant {
+  int block;
+  void (*body)(StepArgs);
+  void (*last)(StepArgs);
+};
+
+#define F32V(B, M, C) {B, k_step_f32<B, M, C, false>, k_step_f32<B, M, C, true>}
+static const F32Variant kF32Variants[] = {
+    F32V(256, 4, false), F32V(256, 5, false), F32V(256, 6, false), F32V(128, 8, false),
+    F32V(128, 12, false), F32V(512, 2, false), F32V(256, 5, true), F32V(128, 12, true),
+};
+#undef F32V
+
+int step_variant_count() { return (int)(sizeof(kF32Variants) / sizeof(kF32Variants[0])); }
+
+int step_variant_block(int v) { return kF32Variants[v].block; }
+
+cudaError_t launch_step(bool f64, bool last, const StepArgs &a, int blocks, cudaStream_t s,
+                        int variant) {
   if (f64) {
     if (last)
       k_step<true, true><<<blocks, STEP_BLOCK, 0, s>>>(a);
     else
       k_step<true, false><<<blocks, STEP_BLOCK, 0, s>>>(a);
   } else {
+    if (variant < 0 || variant >= step_variant_count()) variant = 0;
+    const F32Variant &v = kF32Variants[variant];
+    dim3 grid((a.max_nodes + v.block - 1) / v.block, a.total_clones);
     if (last)
-      k_step<false, true><<<blocks, STEP_BLOCK, 0, s>>>(a);
+      v.last<<<grid, v.block, 0, s>>>(a);
     else
-      k_step<false, false><<<blocks, STEP_BLOCK, 0, s>>>(a);
+      v.body<<<grid, v.block, 0, s>>>(a);
   }
   return cudaGetLastError();
 }

@@ -219,6 +219,17 @@ int clbm_run_sampler(clbm_ctx *ctx, int steps, int intervals, double *rvalues);
 int clbm_profile(clbm_ctx *ctx, int enable);
 int clbm_profile_read(clbm_ctx *ctx, double *step_ms, int *nsteps);
 
+/* Autotuner of the FP32 step kernel: times each launch variant (block size,
+ * registers per thread, store caching) on this context's workload, `launches`
+ * launches each, at an interval boundary without touching the sampler state,
+ * and selects the fastest for the context.  *best = chosen variant,
+ * ms_per_variant (nullable, *nvariants entries) = mean milliseconds per
+ * launch.  With ms_per_variant NULL a result cached for the same lattices and
+ * clone counts is reused.  FP64 contexts have one variant. */
+int clbm_autotune(clbm_ctx *ctx, int launches, int *best,
+                  double *ms_per_variant, int *nvariants);
+int clbm_set_step_variant(clbm_ctx *ctx, int variant);
+
 /* device error word (CLBM_DEV_* bits) accumulated since the last clear */
 int clbm_error_word(clbm_ctx *ctx, unsigned *word, int clear);
 /* block until the context's stream is idle */

@@ -187,3 +187,25 @@ def test_weight_overflow_is_reported(gpu, clbm_lib, orc):
         assert e.value.status == clbm_lib.ERR_DEVICE
         assert s.error_word(clear=True) & 0x2
         assert np.array_equal(s.clone_result(0)["labels"], np.arange(nc))
+
+
+def test_step_variants_are_bit_identical_and_autotune_keeps_state(gpu, clbm_lib, orc):
+    g, phys, T, n, nc, seed = channel_case(orc, W=200, H=50, side=8, nc=6, T=30, n=1, k=0.5)
+    d = desc(clbm_lib, g, nc, perturb_mode=2, eps=1e-4, seed=seed, **phys)
+    drags = []
+    with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T) as s:
+        s.init_equilibrium(0, 0.05, 1e-3, seed)
+        before = s.dump(0, 2)
+        best, ms = s.autotune(launches=2)
+        assert 0 <= best < len(ms) and (ms > 0).all()
+        assert np.array_equal(s.dump(0, 2), before)
+        assert s.error_word() == 0
+    for v in range(len(ms)):
+        with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T) as s:
+            s.init_equilibrium(0, 0.05, 1e-3, seed)
+            s.set_step_variant(v)
+            s.run_interval(T)
+            drags.append(s.drag(0))
+            s.clone_step()
+    for v in range(1, len(drags)):
+        assert np.array_equal(drags[v], drags[0]), v
