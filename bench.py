@@ -299,7 +299,7 @@ def main():
                      "mean_step_ms": step_ms / max(1, nsteps)},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": (wl.steps + 3) * args.steps,
+        "gpu_launches": (wl.steps + 4) * args.steps,
         "clocks": clocks,
         "rvalues_tail": [float(x) for x in rv[:, -1]],
     }

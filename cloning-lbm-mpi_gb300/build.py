@@ -64,6 +64,9 @@ def build_library(verbose: bool = False) -> Path:
     return lib
 
 
+DRIVER_VARIANTS = (("TLGK_LBM", "plain"), ("TLGK_LBM_POPS_PERTURB", "pops"))
+
+
 def build_drivers(verbose: bool = False) -> list[Path]:
     """The three drop-in executables (TLGK_LBM, TLGK_LBM_FORCING,
     TLGK_LBM_POPS_PERTURB), C++ host code over libclbm's C ABI."""
@@ -76,8 +79,7 @@ def build_drivers(verbose: bool = False) -> list[Path]:
     common = [s for s in srcs if s.stem != "tlgk_main"]
     main = DRIVERS / "tlgk_main.cpp"
     jobs = []
-    for name, variant in (("TLGK_LBM", "plain"), ("TLGK_LBM_FORCING", "forcing"),
-                          ("TLGK_LBM_POPS_PERTURB", "pops")):
+    for name, variant in DRIVER_VARIANTS:
         exe = BUILD / name
         outs.append(exe)
         if _stale(exe, srcs + headers + [lib]):

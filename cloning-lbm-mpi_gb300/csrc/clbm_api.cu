@@ -137,7 +137,7 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
   if (!runs || nruns < 1 || nruns > 1024) return fail(CLBM_ERR_INVALID, "nruns out of range");
   if (precision != CLBM_FP64 && precision != CLBM_FP32)
     return fail(CLBM_ERR_INVALID, "unknown precision");
-  if (max_steps < 1) return fail(CLBM_ERR_INVALID, "max_steps < 1");
+  if (max_steps < 1 || max_steps > 65535) return fail(CLBM_ERR_INVALID, "max_steps outside [1, 65535]");
   for (int r = 0; r < nruns; r++) {
     const clbm_run_desc &d = runs[r];
     if (!geometry_ok(d)) return fail(CLBM_ERR_INVALID, "invalid run geometry");

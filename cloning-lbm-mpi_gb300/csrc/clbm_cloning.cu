@@ -12,13 +12,16 @@
 namespace clbm {
 
 // ---------------------------------------------------------------------------
-// One thread per clone: F_t = (West + East + North + South) * scale - shift
-// with each side summed in the reference's node order (force.cpp:23-141,
-// pops driver :445-449), then s = dt * sum_t F_t (:459, :465).
+// Drag of every (clone, step): F_t = (West + East + North + South) * scale -
+// shift, each side summed in the reference's node order (force.cpp:23-141,
+// pops driver :445-449); one thread per (clone, step), clones fastest so the
+// [term][clone] slabs are read coalesced.  Then one thread per clone forms
+// s = dt * sum_t F_t in step order (:459, :465).
 template <bool F64>
-__global__ void k_drag_reduce(DevArrays d, int nruns, int total_clones, int steps) {
+__global__ void k_drag_terms_sum(DevArrays d, int nruns, int total_clones) {
   using T = typename std::conditional<F64, double, float>::type;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.y;
   if (g >= total_clones) return;
   int r = 0;
   while (r + 1 < nruns && g >= d.runs[r + 1].clone_base) r++;
@@ -26,39 +29,45 @@ __global__ void k_drag_reduce(DevArrays d, int nruns, int total_clones, int step
   const int c = g - R.clone_base;
   const int nc = R.nclones;
   const int sy = R.ymax - R.ymin + 1, sx = R.xmax - R.xmin + 1;
-  double *drag = d.drag + (long long)g * d.max_steps;
-  double acc = 0.0;
-  bool bad = false;
-  for (int t = 0; t < steps; t++) {
-    const T *tt = (const T *)d.terms + (long long)t * d.term_slab + R.term_base + c;
-    double side[4];
-    int i = 0;
-    const int len[4] = {sy, sy, sx, sx};
+  const T *tt = (const T *)d.terms + (long long)t * d.term_slab + R.term_base + c;
+  double side[4];
+  int i = 0;
+  const int len[4] = {sy, sy, sx, sx};
 #pragma unroll
-    for (int s = 0; s < 4; s++) {
-      double v = (double)tt[(long long)i * nc];
-      for (int q = 1; q < len[s]; q++) v = DADD(v, (double)tt[(long long)(i + q) * nc]);
-      side[s] = v;
-      i += len[s];
-    }
-    double F = DADD(DADD(DADD(side[0], side[1]), side[2]), side[3]);
-    F = DMUL(F, R.force_scale);
-    F = DSUB(F, R.force_shift);
-    bad |= !isfinite(F);
-    drag[t] = F;
-    acc = t == 0 ? F : DADD(acc, F);
+  for (int s = 0; s < 4; s++) {
+    double v = (double)tt[(long long)i * nc];
+    for (int q = 1; q < len[s]; q++) v = DADD(v, (double)tt[(long long)(i + q) * nc]);
+    side[s] = v;
+    i += len[s];
   }
-  d.sacc[g] = DMUL(acc, R.dt);
-  if (bad) atomicOr(d.err, (unsigned)ERR_NONFINITE_DRAG);
+  double F = DADD(DADD(DADD(side[0], side[1]), side[2]), side[3]);
+  F = DMUL(F, R.force_scale);
+  F = DSUB(F, R.force_shift);
+  if (!isfinite(F)) atomicOr(d.err, (unsigned)ERR_NONFINITE_DRAG);
+  d.drag[(long long)g * d.max_steps + t] = F;
+}
+
+__global__ void k_drag_integrate(DevArrays d, int nruns, int total_clones, int steps) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total_clones) return;
+  int r = 0;
+  while (r + 1 < nruns && g >= d.runs[r + 1].clone_base) r++;
+  const double *drag = d.drag + (long long)g * d.max_steps;
+  double acc = drag[0];
+  for (int t = 1; t < steps; t++) acc = DADD(acc, drag[t]);
+  d.sacc[g] = DMUL(acc, d.runs[r].dt);
 }
 
 cudaError_t launch_drag_reduce(bool f64, const DevArrays &d, int nruns, int total_clones,
                                int steps, cudaStream_t s) {
-  const int blocks = (total_clones + 127) / 128;
+  dim3 grid((total_clones + 127) / 128, steps);
   if (f64)
-    k_drag_reduce<true><<<blocks, 128, 0, s>>>(d, nruns, total_clones, steps);
+    k_drag_terms_sum<true><<<grid, 128, 0, s>>>(d, nruns, total_clones);
   else
-    k_drag_reduce<false><<<blocks, 128, 0, s>>>(d, nruns, total_clones, steps);
+    k_drag_terms_sum<false><<<grid, 128, 0, s>>>(d, nruns, total_clones);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_drag_integrate<<<(total_clones + 127) / 128, 128, 0, s>>>(d, nruns, total_clones, steps);
   return cudaGetLastError();
 }
 
