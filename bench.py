@@ -184,6 +184,55 @@ def run_reference(args, wl, world, rank):
     print(json.dumps(line))
 
 
+def precision_study(args, wl):
+    """FP32 populations vs the FP64 mode (bit-identical to the oracle) on the
+    same GB300 and the same seeds: drag-series error of the first interval,
+    SCGF of every run with the FP32 context following the FP64 genealogy
+    (precision effect only) and running independently (precision plus the
+    genealogy flips it causes), and the speed of both."""
+    import torch
+    import clbm
+    descs = wl.descs()
+    ctx = {k: clbm.Sampler(descs, p, max_steps=wl.steps, flags=clbm.FLAG_GRAPH)
+           for k, p in (("f64", clbm.FP64), ("f32_locked", clbm.FP32), ("f32_free", clbm.FP32))}
+    for s in ctx.values():
+        for i, r in enumerate(wl.runs):
+            s.init_equilibrium(i, r.u0, wl.init_noise, r.seed)
+    n = args.steps
+    secs = {}
+    drag_err = []
+    for t in range(n):
+        for k, s in ctx.items():
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.run_interval(wl.steps)
+            s.sync()
+            secs[k] = secs.get(k, 0.0) + time.perf_counter() - t0
+        if t == 0:
+            for i in range(len(wl.runs)):
+                a, b = ctx["f64"].drag(i), ctx["f32_locked"].drag(i)
+                drag_err.append({"max_rel": float(np.abs(b - a).max() / np.abs(a).max()),
+                                 "rms_rel": float(np.sqrt(np.mean((b - a) ** 2)) / np.sqrt(np.mean(a ** 2)))})
+        for s in ctx.values():
+            s.clone_step()
+        for i in range(len(wl.runs)):
+            ctx["f32_locked"].set_pending_labels(i, ctx["f64"].clone_result(i)["labels"])
+    runs = []
+    for i, r in enumerate(wl.runs):
+        dT = wl.steps * r.dt
+        psi = {k: s.scgf(i, dT) for k, s in ctx.items()}
+        runs.append({"run": i, "k": r.k, "scgf_fp64": psi["f64"],
+                     "scgf_fp32_locked": psi["f32_locked"], "scgf_fp32_free": psi["f32_free"],
+                     "scgf_rel_err_locked": abs(psi["f32_locked"] - psi["f64"]) / abs(psi["f64"]),
+                     "scgf_rel_err_free": abs(psi["f32_free"] - psi["f64"]) / abs(psi["f64"]),
+                     "drag_first_interval": drag_err[i]})
+    lups = wl.lattice_updates_per_interval * n
+    line = {"study": "precision", "workload": wl.name, "intervals": n, "steps_per_interval": wl.steps,
+            "runs": runs, "clone_lups": {k: lups / v for k, v in secs.items()},
+            "fp32_over_fp64_speed": secs["f64"] / secs["f32_free"]}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -193,6 +242,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--graph", action="store_true", help="replay each interval as a CUDA graph")
+    ap.add_argument("--study", choices=["precision"], default=None)
     args = ap.parse_args()
     from clbm import configs
     wl = configs.WORKLOADS[args.workload]()
@@ -200,11 +251,15 @@ def main():
     if args.impl == "reference":
         run_reference(args, wl, world, rank)
         return
+    if args.study == "precision":
+        precision_study(args, wl)
+        return
 
     import torch
     import clbm
     torch.cuda.set_device(local)
-    s = clbm.Sampler(wl.descs(), wl.precision, max_steps=wl.steps)
+    s = clbm.Sampler(wl.descs(), wl.precision, max_steps=wl.steps,
+                     flags=clbm.FLAG_GRAPH if args.graph else 0)
     for i, r in enumerate(wl.runs):
         s.init_equilibrium(i, r.u0, wl.init_noise, r.seed + 1000 * rank)
     stream = torch.cuda.ExternalStream(s.stream())
@@ -218,7 +273,7 @@ def main():
     barrier(world)
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s.profile(True)
+    s.profile(not args.graph)  # event pairs around the step launches (eager replay only)
     with ClockSampler(local) as clk:
         ev0.record(stream)
         rv = s.run_sampler(wl.steps, args.steps)
@@ -226,6 +281,11 @@ def main():
         torch.cuda.synchronize()
     barrier(world)
     ms = allmax(world, ev0.elapsed_time(ev1))
+    if args.graph:
+        # graph replays carry no per-kernel events: time the step launches of
+        # one more, eagerly enqueued interval right after the timed region
+        s.profile(True)
+        s.run_sampler(wl.steps, 1)
     step_ms, nsteps = s.profile_read()
     s.profile(False)
     lups_interval = wl.lattice_updates_per_interval
@@ -300,6 +360,7 @@ def main():
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": (wl.steps + 4) * args.steps,
+        "graph": bool(args.graph),
         "clocks": clocks,
         "rvalues_tail": [float(x) for x in rv[:, -1]],
     }

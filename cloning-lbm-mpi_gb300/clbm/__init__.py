@@ -30,7 +30,8 @@ EXPORTS = [
     "clbm_ref_perturbed_state", "clbm_ref_perturbed_state_noalloc", "clbm_create", "clbm_destroy", "clbm_load_pops_aos_f64",
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
-    "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
+    "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
+    "clbm_set_pending_labels", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -92,6 +93,8 @@ def lib() -> C.CDLL:
         L.clbm_run_sampler.argtypes = [vp, i, i, vp]
         L.clbm_get_rvalues.argtypes = [vp, i, i, i, vp, vp]
         L.clbm_intervals_done.argtypes = [vp, i, C.POINTER(i)]
+        L.clbm_scgf.argtypes = [vp, i, i, i, d, C.POINTER(d)]
+        L.clbm_set_pending_labels.argtypes = [vp, i, vp]
         L.clbm_profile.argtypes = [vp, i]
         L.clbm_autotune.argtypes = [vp, i, C.POINTER(i), vp, C.POINTER(i)]
         L.clbm_set_step_variant.argtypes = [vp, i]
@@ -255,6 +258,17 @@ class Sampler:
         rv, lr = np.empty(count), np.empty(count)
         check(lib().clbm_get_rvalues(self.h, run, first, count, _p(rv), _p(lr)), "clbm_get_rvalues")
         return rv, lr
+
+    def scgf(self, run: int, dT: float, first: int = 0, count: int | None = None) -> float:
+        if count is None:
+            count = self.intervals_done(run) - first
+        out = C.c_double()
+        check(lib().clbm_scgf(self.h, run, first, count, dT, C.byref(out)), "clbm_scgf")
+        return out.value
+
+    def set_pending_labels(self, run: int, labels: np.ndarray):
+        a = np.ascontiguousarray(labels, dtype=np.int32)
+        check(lib().clbm_set_pending_labels(self.h, run, _p(a)), "clbm_set_pending_labels")
 
     def run_sampler(self, steps: int, intervals: int) -> np.ndarray:
         rv = np.empty((len(self.runs), intervals))

@@ -702,3 +702,36 @@ extern "C" int clbm_set_step_variant(clbm_ctx *c, int variant) {
   destroy_graphs(c);
   return CLBM_OK;
 }
+
+extern "C" int clbm_scgf(clbm_ctx *c, int run, int first, int count, double dT, double *psi) {
+  if (int s = check_run(c, run)) return s;
+  if (!psi || count < 1 || !(dT > 0.0)) return fail(CLBM_ERR_INVALID, "need count >= 1, dT > 0, psi");
+  int done = 0;
+  CK(cudaMemcpyAsync(&done, &c->d.state[run].interval, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (first < 0 || first + count > done || first + count > c->d.max_intervals)
+    return fail(CLBM_ERR_INVALID, "requested intervals outside the recorded history");
+  double *d_out = nullptr;
+  CK(cudaMallocAsync((void **)&d_out, sizeof(double), c->stream));
+  cudaError_t e = launch_scgf(c->d.logr + (size_t)run * c->d.max_intervals, first, count, dT, d_out, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(psi, d_out, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(d_out, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return clbm_status_from_cuda(e);
+}
+
+extern "C" int clbm_set_pending_labels(clbm_ctx *c, int run, const int *labels) {
+  if (int s = check_run(c, run)) return s;
+  if (!labels) return fail(CLBM_ERR_INVALID, "labels is NULL");
+  const RunDev &R = c->runs_h[run];
+  std::vector<int> mark(R.nclones);
+  for (int j = 0; j < R.nclones; j++) {
+    if (labels[j] < 0 || labels[j] >= R.nclones) return fail(CLBM_ERR_INVALID, "label out of range");
+    mark[j] = labels[j] != j;
+    if (mark[j] && labels[labels[j]] != labels[j]) return fail(CLBM_ERR_INVALID, "a parent is itself a copy");
+  }
+  CK(cudaMemcpyAsync(c->d.labels + R.clone_base, labels, sizeof(int) * R.nclones, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d.mark + R.clone_base, mark.data(), sizeof(int) * R.nclones, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return CLBM_OK;
+}

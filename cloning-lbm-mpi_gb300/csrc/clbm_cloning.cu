@@ -327,6 +327,22 @@ fail:
   }
 }
 
+// SCGF estimator in FP64 (post_processing/read_rvalue.py:14-20 restated
+// with its hard-coded dT replaced by the run's): psi = sum_t log R_t /
+// (count * dT) over intervals [first, first+count), summed in order.
+__global__ void k_scgf(const double *logr, int first, int count, double dT, double *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double acc = logr[first];
+  for (int t = 1; t < count; t++) acc = DADD(acc, logr[first + t]);
+  out[0] = DDIV(acc, DMUL((double)count, dT));
+}
+
+cudaError_t launch_scgf(const double *logr, int first, int count, double dT, double *out,
+                        cudaStream_t s) {
+  k_scgf<<<1, 32, 0, s>>>(logr, first, count, dT, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_clone(const DevArrays &d, int nruns, cudaStream_t s) {
   k_clone<<<nruns, CLONE_THREADS, 0, s>>>(d, nruns);
   return cudaGetLastError();

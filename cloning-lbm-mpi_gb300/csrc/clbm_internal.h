@@ -92,6 +92,8 @@ cudaError_t launch_perturb_norms(bool f64, const RunDev *runs, int nruns, const 
 cudaError_t launch_drag_reduce(bool f64, const DevArrays &d, int nruns, int total_clones,
                                int steps, cudaStream_t s);
 cudaError_t launch_clone(const DevArrays &d, int nruns, cudaStream_t s);
+cudaError_t launch_scgf(const double *logr, int first, int count, double dT, double *out,
+                        cudaStream_t s);
 cudaError_t launch_init_equilibrium(bool f64, const RunDev *runs, int nruns, int run, void *pop,
                                     double u0, double noise, unsigned long long seed, int blocks,
                                     cudaStream_t s);

@@ -204,6 +204,16 @@ int clbm_get_clone_result(clbm_ctx *ctx, int run, int *labels, double *rvalue,
  * under systematic resampling at a large bias).  Either pointer may be NULL. */
 int clbm_get_rvalues(clbm_ctx *ctx, int run, int first, int count,
                      double *rvalues, double *log_rvalues);
+/* SCGF estimate psi = sum_t log R_t / (count * dT) over the recorded
+ * intervals [first, first+count), in FP64 on the device; dT is the cloning
+ * interval in the weight's time unit (steps * dt).  The reference computes
+ * it offline (post_processing/read_rvalue.py:14-20, with a hard-coded dT). */
+int clbm_scgf(clbm_ctx *ctx, int run, int first, int count, double dT,
+              double *psi);
+/* Replace the pending copy table of a run (labels[j] = parent slot of slot
+ * j, parents must map to themselves); slots with labels[j] != j become new
+ * clones.  Used to drive two contexts (FP32 and FP64) along one genealogy. */
+int clbm_set_pending_labels(clbm_ctx *ctx, int run, const int *labels);
 /* number of cloning steps a run has completed */
 int clbm_intervals_done(clbm_ctx *ctx, int run, int *done);
 /* `intervals` x (run_interval + clone_step) without host round trips, as

@@ -209,3 +209,25 @@ def test_step_variants_are_bit_identical_and_autotune_keeps_state(gpu, clbm_lib,
             s.clone_step()
     for v in range(1, len(drags)):
         assert np.array_equal(drags[v], drags[0]), v
+
+
+def test_scgf_and_genealogy_lock(gpu, clbm_lib, orc):
+    g, phys, T, n, nc, seed = channel_case(orc, k=3.0, n=4)
+    d = desc(clbm_lib, g, nc, perturb_mode=2, eps=1e-4, seed=seed, **phys)
+    states = np.concatenate([orc.init_equilibrium(g, 0.05, 1e-3, seed, 0, j) for j in range(nc)])
+    ref = orc.run_sampler(g, states, steps=T, intervals=n, perturb_mode=2, eps=1e-4, seed=seed, **phys)
+    dT = T * phys["dt"]
+    with clbm_lib.Sampler([d], clbm_lib.FP64, max_steps=T) as a, clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T) as b:
+        a.load_run(0, states)
+        b.load_run(0, states)
+        for t in range(n):
+            a.run_interval(T)
+            b.run_interval(T)
+            a.clone_step()
+            b.clone_step()
+            b.set_pending_labels(0, a.clone_result(0)["labels"])   # FP32 follows the FP64 genealogy
+        psi = a.scgf(0, dT)
+        expect = np.sum(ref["logr"]) / (n * dT)
+        assert abs(psi - expect) <= 1e-13 * abs(expect)
+        psi32 = b.scgf(0, dT)
+        assert abs(psi32 - psi) <= 1e-4 * abs(psi)
