@@ -66,6 +66,7 @@ struct clbm_ctx {
   int ev_used = 0;
   int prof_steps = 0;
   int max_nodes = 0;
+  int total_tiles[3] = {0, 0, 0};
   int step_variant = 0;  // FP32 step launch variant (clbm_autotune)
 };
 
@@ -183,6 +184,19 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
     R.nterms = 2 * (d.ymax - d.ymin + 1) + 2 * (d.xmax - d.xmin + 1);
     R.div_w = (unsigned)(((1ULL << 32) + (unsigned long long)d.width - 1) / (unsigned long long)d.width);
     R.plane = ((long long)R.nodes + 63) / 64 * 64;
+    for (int q = 0; q < 3; q++) {
+      const int tb = 128 << q;
+      R.tiles[q] = (R.nodes + tb - 1) / tb;
+      // clone = umulhi(local tile, ceil(2^32/tiles)) is exact while
+      // local * (tiles - 1) < 2^32
+      if ((unsigned long long)d.nclones * R.tiles[q] * (unsigned long long)(R.tiles[q] - 1) >= (1ULL << 32)) {
+        delete c;
+        return fail(CLBM_ERR_INVALID, "too many clones for the lattice size in one run (clones * tiles^2 >= 2^32)");
+      }
+      R.tiles_div[q] = (unsigned)(((1ULL << 32) + R.tiles[q] - 1) / R.tiles[q]);
+      R.tile_base[q] = c->total_tiles[q];
+      c->total_tiles[q] += d.nclones * R.tiles[q];
+    }
     R.pop_base = pop;
     R.term_base = terms;
     R.snap_base = snaps;
@@ -403,7 +417,8 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
   }
   for (int t = 0; t < steps; t++) {
     StepArgs a{c->d.runs, c->nruns, t, c->pop[cur], c->pop[1 - cur], c->d.terms, c->d.term_slab,
-               c->d.err, c->total_clones, c->max_nodes};
+               c->d.err, c->total_clones, c->max_nodes,
+               {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}};
     if ((e = launch_step(f64, t == steps - 1, a, c->total_blocks, s, c->step_variant)) != cudaSuccess)
       return e;
     cur = 1 - cur;
@@ -662,7 +677,8 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
   double best_ms = 1e30;
   for (int v = 0; v < nv; v++) {
     StepArgs a{c->d.runs, c->nruns, 0, c->pop[c->s_buf], c->pop[1 - c->s_buf], c->d.terms,
-               c->d.term_slab, c->d.err, c->total_clones, c->max_nodes};
+               c->d.term_slab, c->d.err, c->total_clones, c->max_nodes,
+               {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}};
     cudaError_t e = launch_step(false, false, a, c->total_blocks, c->stream, v);  // warm-up
     if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
     for (int i = 0; i < launches && e == cudaSuccess; i++)

@@ -46,6 +46,11 @@ struct RunDev {
   int nodes;                   // W*H
   unsigned div_w;              // ceil(2^32 / W): y = umulhi(n, div_w)
   int pad_;
+  // tile tables of the FP32 step for tiles of 128 / 256 / 512 nodes: first
+  // block of this run, tiles per clone and ceil(2^32 / tiles)
+  int tile_base[3];
+  int tiles[3];
+  unsigned tiles_div[3];
   long long pop_base;          // element offset of this run's clone 0
   long long plane;             // elements per population plane (padded)
   long long term_base;         // offset of this run in a step's term slab

@@ -61,8 +61,9 @@ struct StepArgs {
   void *terms;        // base of the term slabs
   long long term_slab;
   unsigned *err;
-  int total_clones;   // grid y of the FP32 step
-  int max_nodes;      // largest W*H of the runs (grid x = tiles of it)
+  int total_clones;
+  int max_nodes;
+  int total_tiles[3]; // FP32 step grid for tiles of 128 / 256 / 512 nodes
 };
 
 struct ReseedArgs {

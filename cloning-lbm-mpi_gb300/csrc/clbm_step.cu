@@ -166,14 +166,22 @@ __global__ void __launch_bounds__(STEP_BLOCK) k_step(StepArgs a) {
 // no node on a wall row or in the square's bounding box (the bulk) take a
 // path without any bounce-back selects; the decision is warp-uniform.
 // Collision by opposite pairs (collide_f32_pairs).
+template <int BLOCK>
+__device__ __forceinline__ constexpr int tile_slot() {
+  return BLOCK == 128 ? 0 : (BLOCK == 256 ? 1 : 2);
+}
+
 template <int BLOCK, int MINB, bool CS, bool LAST>
 __global__ void __launch_bounds__(BLOCK, MINB) k_step_f32(StepArgs a) {
-  const int gclone = blockIdx.y;
+  constexpr int TS = tile_slot<BLOCK>();
+  const int b = blockIdx.x;
   int r = 0;
-  while (r + 1 < a.nruns && gclone >= a.runs[r + 1].clone_base) r++;
+  while (r + 1 < a.nruns && b >= a.runs[r + 1].tile_base[TS]) r++;
   const RunDev &R = a.runs[r];
-  const int clone = gclone - R.clone_base;
-  const int n = blockIdx.x * BLOCK + threadIdx.x;
+  const unsigned local = (unsigned)(b - R.tile_base[TS]);
+  const int clone = (int)__umulhi(local, R.tiles_div[TS]);
+  const int tile = (int)local - clone * R.tiles[TS];
+  const int n = tile * BLOCK + threadIdx.x;
   const int W = R.W, H = R.H;
   const bool valid = n < R.nodes;
   const int y = (int)__umulhi((unsigned)n, R.div_w);
@@ -266,7 +274,8 @@ cudaError_t launch_step(bool f64, bool last, const StepArgs &a, int blocks, cuda
   } else {
     if (variant < 0 || variant >= step_variant_count()) variant = 0;
     const F32Variant &v = kF32Variants[variant];
-    dim3 grid((a.max_nodes + v.block - 1) / v.block, a.total_clones);
+    const int ts = v.block == 128 ? 0 : (v.block == 256 ? 1 : 2);
+    const int grid = a.total_tiles[ts];
     if (last)
       v.last<<<grid, v.block, 0, s>>>(a);
     else
