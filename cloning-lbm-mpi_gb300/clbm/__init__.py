@@ -31,7 +31,7 @@ EXPORTS = [
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
-    "clbm_set_pending_labels", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
+    "clbm_set_pending_labels", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -95,6 +95,9 @@ def lib() -> C.CDLL:
         L.clbm_intervals_done.argtypes = [vp, i, C.POINTER(i)]
         L.clbm_scgf.argtypes = [vp, i, i, i, d, C.POINTER(d)]
         L.clbm_set_pending_labels.argtypes = [vp, i, vp]
+        L.clbm_drag_fwd.argtypes = [vp, i, i, vp]
+        L.clbm_drag_bwd.argtypes = [vp]
+        L.clbm_get_drag_grad_aos_f64.argtypes = [vp, i, i, vp]
         L.clbm_profile.argtypes = [vp, i]
         L.clbm_autotune.argtypes = [vp, i, C.POINTER(i), vp, C.POINTER(i)]
         L.clbm_set_step_variant.argtypes = [vp, i]
@@ -265,6 +268,20 @@ class Sampler:
         out = C.c_double()
         check(lib().clbm_scgf(self.h, run, first, count, dT, C.byref(out)), "clbm_scgf")
         return out.value
+
+    def drag_fwd(self, steps: int, every: int) -> np.ndarray:
+        J = np.empty(sum(r.nclones for r in self.runs))
+        check(lib().clbm_drag_fwd(self.h, steps, every, _p(J)), "clbm_drag_fwd")
+        self.last_steps = steps
+        return J
+
+    def drag_bwd(self):
+        check(lib().clbm_drag_bwd(self.h), "clbm_drag_bwd")
+
+    def drag_grad(self, run: int, clone: int) -> np.ndarray:
+        out = np.empty(self.n(run))
+        check(lib().clbm_get_drag_grad_aos_f64(self.h, run, clone, _p(out)), "clbm_get_drag_grad_aos_f64")
+        return out
 
     def set_pending_labels(self, run: int, labels: np.ndarray):
         a = np.ascontiguousarray(labels, dtype=np.int32)

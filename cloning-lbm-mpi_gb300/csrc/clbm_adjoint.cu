@@ -1,0 +1,218 @@
+// clbm_adjoint.cu -- discrete adjoint of the interval-integrated drag.
+//
+// Forward (as in clbm_step.cu): P_0 = C(S_0); for t = 0..T-1:
+// S_{t+1} = Pull(P_t), F_t = D(S_{t+1}), P_{t+1} = C(S_{t+1});
+// J = kappa * sum_t D(S_{t+1}), kappa = dt * force_scale (the weight
+// integral s of src/mpi_LBM_GK_pops_perturb.cpp:445-465; the constant shift
+// has no gradient).  Adjoint, sigma_t = dJ/dS_t:
+//   sigma_T = kappa grad D(S_T)
+//   sigma_t = J_C(S_t)^T Pull^T sigma_{t+1} + kappa grad D(S_t),  1 <= t < T
+//   sigma_0 = J_C(S_0)^T Pull^T sigma_1
+// Pull^T is a gather too: P(m,k) is read by exactly one slot, the node's own
+// (m, opp k) when that slot is bounced back, else (m + c_k, k); square-interior
+// nodes carry no sensitivity (they are reset every step).  The collision
+// Jacobian is a rank-3 update of (1-omega) I through rho, jx, jy, so its
+// transpose costs three reductions per node.  D is the stress-integration drag
+// (src/lbm_src/force.cpp:8-144) with Pi_xx^neq = sum_{cx!=0} f - rho/3 - jx^2/rho
+// and Pi_xy^neq = f5 - f6 + f7 - f8 - jx jy / rho (its closed form).
+#include "clbm_internal.h"
+#include "clbm_physics.cuh"
+
+namespace clbm {
+
+template <bool F64>
+using real_t = typename std::conditional<F64, double, float>::type;
+
+struct AdjArgs {
+  const RunDev *runs;
+  int nruns;
+  const void *sigma_in;  // sigma_{t+1}
+  void *sigma_out;       // sigma_t
+  const void *P;         // P_{t-1} (pulled into S_t), or S_0 when from_s0
+  int with_drag;         // add kappa grad D(S_t)
+  int from_s0;
+};
+
+__device__ __forceinline__ int adj_locate(const RunDev *runs, int nruns, int &clone, int &n) {
+  const int b = blockIdx.x;
+  int r = 0;
+  while (r + 1 < nruns && b >= runs[r + 1].block_base) r++;
+  const RunDev &R = runs[r];
+  const int local = b - R.block_base;
+  clone = local / R.blocks_per_clone;
+  n = (local - clone * R.blocks_per_clone) * blockDim.x + threadIdx.x;
+  return r;
+}
+
+// gradient of this node's drag contribution w.r.t. its nine populations
+// (f or g = f - w, the same derivative), times kappa
+template <typename T>
+__device__ __forceinline__ void drag_grad(const RunDev &R, int x, int y, const T S[9], T kappa,
+                                          T out[9]) {
+  T rho, jx = (S[1] - S[3]) + ((S[5] - S[7]) + (S[8] - S[6]));
+  T jy = (S[2] - S[4]) + ((S[5] - S[7]) + (S[6] - S[8]));
+  T sum = ((S[0] + (S[1] + S[3])) + (S[2] + S[4])) + ((S[5] + S[7]) + (S[6] + S[8]));
+  rho = (sizeof(T) == 8 ? sum : T(1) + sum);
+  const T ux = jx / rho, uy = jy / rho;
+  const T c = (T)R.cforce;
+  T wx = 0, wxy = 0;  // weights of dPi_xx and dPi_xy
+  T wr = 0;           // weight of d(rho/3)
+  if (x == R.xmin) { wr += T(1); wx += c; }
+  if (x == R.xmax) { wr -= T(1); wx -= c; }
+  if (y == R.ymax) wxy -= c;
+  if (y == R.ymin) wxy += c;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const T cx = (T)cx_of(k), cy = (T)cy_of(k);
+    const T dpxx = (cx != T(0) ? T(1) : T(0)) - T(1) / T(3) - (T(2) * ux * cx - ux * ux);
+    const T dpxy = cx * cy - cx * uy - cy * ux + ux * uy;
+    out[k] = kappa * (wr * (T(1) / T(3)) + wx * dpxx + wxy * dpxy);
+  }
+}
+
+// sigma_S = J_C(S)^T pi for the BGK + Guo collision of clbm_physics.cuh
+template <typename T>
+__device__ __forceinline__ void collide_adjoint(const RunDev &R, const T S[9], const T pi[9],
+                                                T out[9]) {
+  const T omega = (T)R.omega, om1 = T(1) - omega, beta = (T)R.beta;
+  const T cf = (T)R.cforce;
+  T sum = ((S[0] + (S[1] + S[3])) + (S[2] + S[4])) + ((S[5] + S[7]) + (S[6] + S[8]));
+  const T rho = (sizeof(T) == 8 ? sum : T(1) + sum);
+  const T jx = (S[1] - S[3]) + ((S[5] - S[7]) + (S[8] - S[6]));
+  const T jy = (S[2] - S[4]) + ((S[5] - S[7]) + (S[6] - S[8]));
+  const T ux = (jx + T(0.5) * beta) / rho, uy = jy / rho;
+  const T u2 = T(1.5) * (ux * ux + uy * uy);
+  T G0 = 0, Gx = 0, Gy = 0;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const T cx = (T)cx_of(k), cy = (T)cy_of(k), w = (T)w_of(k);
+    const T e = cx * ux + cy * uy;
+    const T dfeq_drho = w * (T(1) + T(3) * e + T(4.5) * e * e - u2);
+    const T dG_dux = omega * w * rho * (T(3) * cx + T(9) * e * cx - T(3) * ux) +
+                     w * cf * beta * (T(-3) + T(9) * cx * cx);
+    const T dG_duy = omega * w * rho * (T(3) * cy + T(9) * e * cy - T(3) * uy) +
+                     w * cf * beta * (T(9) * cx * cy);
+    G0 += pi[k] * omega * dfeq_drho;
+    Gx += pi[k] * dG_dux;
+    Gy += pi[k] * dG_duy;
+  }
+  const T A = G0 - (ux * Gx + uy * Gy) / rho;
+  const T Bx = Gx / rho, By = Gy / rho;
+#pragma unroll
+  for (int k = 0; k < 9; k++) out[k] = om1 * pi[k] + A + (T)cx_of(k) * Bx + (T)cy_of(k) * By;
+}
+
+template <bool F64>
+__global__ void __launch_bounds__(STEP_BLOCK) k_adj_step(AdjArgs a) {
+  using T = real_t<F64>;
+  int clone, n;
+  const int r = adj_locate(a.runs, a.nruns, clone, n);
+  const RunDev &R = a.runs[r];
+  if (n >= R.nodes || clone >= R.nclones) return;
+  const long long plane = R.plane;
+  const long long cb = R.pop_base + (long long)clone * 9 * plane;
+  const T *sig = (const T *)a.sigma_in + cb;
+  const T *P = (const T *)a.P + cb;
+  T *out = (T *)a.sigma_out + cb;
+  const int W = R.W, y = n / W, x = n - y * W;
+  const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+  const int mask = (in_box || y == 0 || y == R.H - 1) ? bounce_mask(R, x, y) : 0;
+  if (mask & 512) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) out[k * plane + n] = T(0);
+    return;
+  }
+  const int xl = (x == 0) ? W - 1 : x - 1, xr = (x == W - 1) ? 0 : x + 1;
+  const int row = y * W;
+  T S[9], pi[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const int cx = cx_of(k), cy = cy_of(k);
+    // S_t(n,k) = P_{t-1}(n - c_k, k), or P_{t-1}(n, opp k) when bounced
+    if (a.from_s0) {
+      S[k] = P[k * plane + n];
+    } else {
+      const int sx = cx == 1 ? xl : (cx == -1 ? xr : x);
+      const int srow = cy == 1 ? row - W : (cy == -1 ? row + W : row);
+      S[k] = ((mask >> k) & 1) ? P[opp_of(k) * plane + n] : P[k * plane + srow + sx];
+    }
+    // P(n,k) is read by slot (n, opp k) when that slot bounces, else by (n + c_k, k)
+    const int ok = opp_of(k);
+    if ((mask >> ok) & 1) {
+      pi[k] = sig[ok * plane + n];
+    } else {
+      const int tx = cx == 1 ? xr : (cx == -1 ? xl : x);
+      const int trow = cy == 1 ? row + W : (cy == -1 ? row - W : row);
+      pi[k] = sig[k * plane + trow + tx];
+    }
+  }
+  T o[9];
+  collide_adjoint<T>(R, S, pi, o);
+  if (a.with_drag && in_box) {
+    T dg[9];
+    drag_grad<T>(R, x, y, S, (T)(R.dt * R.force_scale), dg);
+#pragma unroll
+    for (int k = 0; k < 9; k++) o[k] += dg[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) out[k * plane + n] = o[k];
+}
+
+// sigma_T = kappa grad D(Pull(P_{T-1})), zero away from the perimeter
+template <bool F64>
+__global__ void __launch_bounds__(STEP_BLOCK) k_adj_init(AdjArgs a) {
+  using T = real_t<F64>;
+  int clone, n;
+  const int r = adj_locate(a.runs, a.nruns, clone, n);
+  const RunDev &R = a.runs[r];
+  if (n >= R.nodes || clone >= R.nclones) return;
+  const long long plane = R.plane;
+  const long long cb = R.pop_base + (long long)clone * 9 * plane;
+  const T *P = (const T *)a.P + cb;
+  T *out = (T *)a.sigma_out + cb;
+  const int W = R.W, y = n / W, x = n - y * W;
+  const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+  const int mask = in_box ? bounce_mask(R, x, y) : 0;
+  if (!in_box || (mask & 512)) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) out[k * plane + n] = T(0);
+    return;
+  }
+  const int xl = (x == 0) ? W - 1 : x - 1, xr = (x == W - 1) ? 0 : x + 1;
+  const int row = y * W;
+  T S[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const int cx = cx_of(k), cy = cy_of(k);
+    const int sx = cx == 1 ? xl : (cx == -1 ? xr : x);
+    const int srow = cy == 1 ? row - W : (cy == -1 ? row + W : row);
+    S[k] = ((mask >> k) & 1) ? P[opp_of(k) * plane + n] : P[k * plane + srow + sx];
+  }
+  T dg[9];
+  drag_grad<T>(R, x, y, S, (T)(R.dt * R.force_scale), dg);
+#pragma unroll
+  for (int k = 0; k < 9; k++) out[k * plane + n] = dg[k];
+}
+
+cudaError_t launch_adj_init(bool f64, const RunDev *runs, int nruns, const void *P, void *sigma,
+                            int blocks, cudaStream_t s) {
+  AdjArgs a{runs, nruns, nullptr, sigma, P, 1, 0};
+  if (f64)
+    k_adj_init<true><<<blocks, STEP_BLOCK, 0, s>>>(a);
+  else
+    k_adj_init<false><<<blocks, STEP_BLOCK, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_step(bool f64, const RunDev *runs, int nruns, const void *sigma_in,
+                            void *sigma_out, const void *P, bool with_drag, bool from_s0,
+                            int blocks, cudaStream_t s) {
+  AdjArgs a{runs, nruns, sigma_in, sigma_out, P, with_drag ? 1 : 0, from_s0 ? 1 : 0};
+  if (f64)
+    k_adj_step<true><<<blocks, STEP_BLOCK, 0, s>>>(a);
+  else
+    k_adj_step<false><<<blocks, STEP_BLOCK, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace clbm

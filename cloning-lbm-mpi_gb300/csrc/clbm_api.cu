@@ -68,6 +68,15 @@ struct clbm_ctx {
   int max_nodes = 0;
   int total_tiles[3] = {0, 0, 0};
   int step_variant = 0;  // FP32 step launch variant (clbm_autotune)
+  bool pending = false;  // a clone step's copies/perturbations await the next interval
+  int *d_zeros = nullptr;
+  // adjoint: forward checkpoints of P every adj_every steps
+  struct {
+    int steps = 0, every = 0;
+    char *s0 = nullptr, *ckpt = nullptr, *seg = nullptr, *sig[2] = {nullptr, nullptr};
+    size_t nckpt = 0, nseg = 0;
+    int result = -1;  // which sig buffer holds sigma_0 after the backward
+  } adj;
 };
 
 extern "C" const char *clbm_strerror(int status) {
@@ -116,7 +125,8 @@ extern "C" int clbm_destroy(clbm_ctx *c) {
   void *bufs[] = {c->pop[0], c->pop[1], c->d.runs, c->d.state, c->d.sacc, c->d.drag, c->d.weights,
                   c->d.labels, c->d.mark, c->d.copies_pre, c->d.copies_post, c->d.prefactors,
                   c->d.pert, c->d.partials, c->d.scratch_i, c->d.scratch_d, c->d.snaps,
-                  c->d.rvalues, c->d.logr, c->d.err, c->d.terms, c->d_identity};
+                  c->d.rvalues, c->d.logr, c->d.err, c->d.terms, c->d_identity, c->d_zeros,
+                  c->adj.s0, c->adj.ckpt, c->adj.seg, c->adj.sig[0], c->adj.sig[1]};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -272,6 +282,8 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
   if ((e = dalloc(D.err, 1)) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&D.terms, (size_t)terms * max_steps * c->elem_size)) != cudaSuccess) return bail(e);
   if ((e = dalloc(c->d_identity, clones)) != cudaSuccess) return bail(e);
+  if ((e = dalloc(c->d_zeros, clones)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemset(c->d_zeros, 0, sizeof(int) * clones)) != cudaSuccess) return bail(e);
 
   std::vector<RunState> st(nruns);
   std::vector<int> ident(clones);
@@ -452,6 +464,7 @@ extern "C" int clbm_run_interval(clbm_ctx *c, int steps) {
   CK(enqueue_interval(c, steps, c->s_buf, c->profiling));
   c->s_buf = sbuf_after(c->s_buf, steps);
   c->last_steps = steps;
+  c->pending = false;
   return CLBM_OK;
 }
 
@@ -471,6 +484,7 @@ extern "C" int clbm_clone_step(clbm_ctx *c) {
   if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
   if (c->last_steps < 1) return fail(CLBM_ERR_INVALID, "clone step before any interval");
   CK(launch_clone(c->d, c->nruns, c->stream));
+  c->pending = true;
   return check_error_word(c);
 }
 
@@ -578,6 +592,7 @@ extern "C" int clbm_run_sampler(clbm_ctx *c, int steps, int intervals, double *r
     }
     c->s_buf = sbuf_after(c->s_buf, steps);
     c->last_steps = steps;
+    c->pending = true;
   }
   if (int st = check_error_word(c)) return st;
   if (rvalues && intervals > 0) {
@@ -746,8 +761,117 @@ extern "C" int clbm_set_pending_labels(clbm_ctx *c, int run, const int *labels) 
     mark[j] = labels[j] != j;
     if (mark[j] && labels[labels[j]] != labels[j]) return fail(CLBM_ERR_INVALID, "a parent is itself a copy");
   }
+  c->pending = true;
   CK(cudaMemcpyAsync(c->d.labels + R.clone_base, labels, sizeof(int) * R.nclones, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->d.mark + R.clone_base, mark.data(), sizeof(int) * R.nclones, cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return CLBM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of the interval-integrated drag (kernels in clbm_adjoint.cu).
+static cudaError_t adj_reserve(char *&p, size_t &have, size_t need) {
+  if (have >= need && p) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  have = 0;
+  cudaError_t e = cudaMalloc((void **)&p, need);
+  if (e == cudaSuccess) have = need;
+  return e;
+}
+
+extern "C" int clbm_drag_fwd(clbm_ctx *c, int steps, int every, double *J) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  if (steps < 1 || steps > c->max_steps || every < 1) return fail(CLBM_ERR_INVALID, "bad steps / checkpoint period");
+  if (c->pending) return fail(CLBM_ERR_INVALID, "a clone step is pending; run an interval first");
+  const bool f64 = c->precision == CLBM_FP64;
+  const size_t pop = c->pop_elems * c->elem_size;
+  const size_t nckpt = (size_t)(steps + every - 1) / every;
+  size_t have_s0 = c->adj.s0 ? pop : 0, have_ck = c->adj.nckpt * pop, have_seg = c->adj.nseg * pop;
+  size_t have_sig0 = c->adj.sig[0] ? pop : 0, have_sig1 = c->adj.sig[1] ? pop : 0;
+  CK(adj_reserve(c->adj.s0, have_s0, pop));
+  CK(adj_reserve(c->adj.ckpt, have_ck, nckpt * pop));
+  c->adj.nckpt = have_ck / pop;
+  CK(adj_reserve(c->adj.seg, have_seg, (size_t)every * pop));
+  c->adj.nseg = have_seg / pop;
+  CK(adj_reserve(c->adj.sig[0], have_sig0, pop));
+  CK(adj_reserve(c->adj.sig[1], have_sig1, pop));
+  cudaStream_t s = c->stream;
+  CK(cudaMemcpyAsync(c->adj.s0, c->pop[c->s_buf], pop, cudaMemcpyDeviceToDevice, s));
+  auto loc = [&](int t) -> char * {
+    return (t % every == 0) ? c->adj.ckpt + (size_t)(t / every) * pop : c->adj.sig[t % 2];
+  };
+  ReseedArgs ra{c->d.runs, c->nruns, c->adj.s0, loc(0), c->d_identity, c->d_zeros, c->d.pert,
+                c->d.prefactors, c->d.snaps, c->d.state, c->d.err};
+  CK(launch_reseed(f64, ra, c->total_blocks, s));
+  for (int t = 0; t < steps; t++) {
+    char *dst = (t + 1 < steps) ? loc(t + 1) : c->adj.sig[(t + 1) % 2];
+    StepArgs a{c->d.runs, c->nruns, t, loc(t), dst, c->d.terms, c->d.term_slab, c->d.err,
+               c->total_clones, c->max_nodes, {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}};
+    CK(launch_step(f64, false, a, c->total_blocks, s, c->step_variant));
+  }
+  CK(launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, s));
+  if (J) CK(cudaMemcpyAsync(J, c->d.sacc, sizeof(double) * c->total_clones, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  c->adj.steps = steps;
+  c->adj.every = every;
+  c->adj.result = -1;
+  c->last_steps = steps;  // clbm_get_drag returns this forward's drag series
+  return check_error_word(c);
+}
+
+extern "C" int clbm_drag_bwd(clbm_ctx *c) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  if (c->adj.steps < 1) return fail(CLBM_ERR_INVALID, "clbm_drag_bwd before clbm_drag_fwd");
+  const bool f64 = c->precision == CLBM_FP64;
+  const size_t pop = c->pop_elems * c->elem_size;
+  const int T = c->adj.steps, C = c->adj.every;
+  cudaStream_t s = c->stream;
+  const int nseg = (T + C - 1) / C;
+  int cur = 0;  // sig[cur] holds sigma_{t+1}
+  auto segP = [&](int lo, int p) -> char * {
+    return p == lo ? c->adj.ckpt + (size_t)(lo / C) * pop : c->adj.seg + (size_t)(p - lo) * pop;
+  };
+  for (int k = nseg - 1; k >= 0; k--) {
+    const int lo = k * C, hi = std::min(lo + C, T) - 1;
+    for (int p = lo; p < hi; p++) {  // recompute P_lo .. P_hi from the checkpoint
+      StepArgs a{c->d.runs, c->nruns, 0, segP(lo, p), segP(lo, p + 1), c->d.terms, c->d.term_slab,
+                 c->d.err, c->total_clones, c->max_nodes,
+                 {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}};
+      CK(launch_step(f64, false, a, c->total_blocks, s, c->step_variant));
+    }
+    for (int p = hi; p >= lo; p--) {
+      if (p == T - 1) {
+        CK(launch_adj_init(f64, c->d.runs, c->nruns, segP(lo, p), c->adj.sig[cur], c->total_blocks, s));
+      } else {
+        CK(launch_adj_step(f64, c->d.runs, c->nruns, c->adj.sig[cur], c->adj.sig[1 - cur], segP(lo, p),
+                           true, false, c->total_blocks, s));
+        cur = 1 - cur;
+      }
+    }
+  }
+  CK(launch_adj_step(f64, c->d.runs, c->nruns, c->adj.sig[cur], c->adj.sig[1 - cur], c->adj.s0, false,
+                     true, c->total_blocks, s));
+  c->adj.result = 1 - cur;
+  CK(cudaStreamSynchronize(s));
+  return check_error_word(c);
+}
+
+extern "C" int clbm_get_drag_grad_aos_f64(clbm_ctx *c, int run, int clone, double *aos) {
+  if (int st = check_run(c, run)) return st;
+  const RunDev &R = c->runs_h[run];
+  if (clone < 0 || clone >= R.nclones || !aos) return fail(CLBM_ERR_INVALID, "bad clone or NULL array");
+  if (c->adj.result < 0) return fail(CLBM_ERR_INVALID, "no gradient: call clbm_drag_bwd first");
+  const size_t n = 9 * (size_t)R.nodes;
+  double *stage = nullptr;
+  CK(cudaMallocAsync((void **)&stage, n * 8, c->stream));
+  cudaError_t e = launch_soa_to_aos(c->precision == CLBM_FP64, c->d.runs, run, clone,
+                                    c->adj.sig[c->adj.result], stage, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(aos, stage, n * 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(stage, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return clbm_status_from_cuda(e);
+  if (c->precision != CLBM_FP64)  // soa_to_aos adds back w[k] for states; a gradient has no shift
+    for (size_t i = 0; i < n; i++) aos[i] -= w_of((int)(i % 9));
   return CLBM_OK;
 }

@@ -93,6 +93,11 @@ cudaError_t launch_perturb_norms(bool f64, const RunDev *runs, int nruns, const 
 cudaError_t launch_drag_reduce(bool f64, const DevArrays &d, int nruns, int total_clones,
                                int steps, cudaStream_t s);
 cudaError_t launch_clone(const DevArrays &d, int nruns, cudaStream_t s);
+cudaError_t launch_adj_init(bool f64, const RunDev *runs, int nruns, const void *P, void *sigma,
+                            int blocks, cudaStream_t s);
+cudaError_t launch_adj_step(bool f64, const RunDev *runs, int nruns, const void *sigma_in,
+                            void *sigma_out, const void *P, bool with_drag, bool from_s0,
+                            int blocks, cudaStream_t s);
 cudaError_t launch_scgf(const double *logr, int first, int count, double dT, double *out,
                         cudaStream_t s);
 cudaError_t launch_init_equilibrium(bool f64, const RunDev *runs, int nruns, int run, void *pop,

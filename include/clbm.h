@@ -240,6 +240,23 @@ int clbm_autotune(clbm_ctx *ctx, int launches, int *best,
                   double *ms_per_variant, int *nvariants);
 int clbm_set_step_variant(clbm_ctx *ctx, int variant);
 
+/* ---- differentiation: adjoint of the interval-integrated drag ------------
+ * J_j = dt * sum_{t<steps} (F_t*force_scale - force_shift) of every clone j
+ * (the weight integral s_j of the sampler, pops driver :445-465), started
+ * from the clones' current states S_0.  clbm_drag_fwd runs the forward in the
+ * context's precision, keeping the post-collision populations every `every`
+ * steps as checkpoints, and returns J (HOST array, all clones of all runs in
+ * run order; nullable).  It does not change the sampler state; it needs no
+ * pending clone step (run an interval first).  clbm_drag_bwd runs the
+ * hand-written adjoint backwards, recomputing each checkpoint segment, and
+ * leaves dJ/dS_0 on the device; clbm_get_drag_grad_aos_f64 returns one
+ * clone's gradient in the reference AoS layout (FP64, 9*Dx*Dy values; zero
+ * inside the square).  dJ/dS_0 is the gradient with respect to an additive
+ * perturbation of the populations. */
+int clbm_drag_fwd(clbm_ctx *ctx, int steps, int every, double *J);
+int clbm_drag_bwd(clbm_ctx *ctx);
+int clbm_get_drag_grad_aos_f64(clbm_ctx *ctx, int run, int clone, double *aos);
+
 /* device error word (CLBM_DEV_* bits) accumulated since the last clear */
 int clbm_error_word(clbm_ctx *ctx, unsigned *word, int clear);
 /* block until the context's stream is idle */
