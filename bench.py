@@ -233,6 +233,57 @@ def precision_study(args, wl):
     print(json.dumps(line))
 
 
+def adjoint_study(args, wl, directions: int = 32, every: int = 20, eps: float = 1e-6):
+    """Gradient of the interval-integrated drag w.r.t. a Gaussian (sigma =
+    1e-4) perturbation of all nine populations: FP32 (and FP64) adjoint
+    against FP64 central finite differences along random directions."""
+    import torch
+    import clbm
+    r = wl.runs[0]
+    descs = wl.descs()
+    T = wl.steps
+    n = 9 * r.nodes
+    rng = np.random.default_rng(r.seed)
+    with clbm.Sampler(descs, clbm.FP64, max_steps=T) as f64:
+        f64.init_equilibrium(0, r.u0, 1e-3, r.seed)
+        base = np.concatenate([f64.dump(0, j) for j in range(r.nclones)])
+    S0 = base + rng.normal(0.0, r.noise, base.size)
+    out = {}
+    grads = {}
+    for name, prec in (("fp32", clbm.FP32), ("fp64", clbm.FP64)):
+        with clbm.Sampler(descs, prec, max_steps=T) as s:
+            s.load_run(0, S0)
+            s.drag_fwd(T, every)  # warm-up
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            J = s.drag_fwd(T, every)
+            t1 = time.perf_counter()
+            s.drag_bwd()
+            t2 = time.perf_counter()
+            grads[name] = np.concatenate([s.drag_grad(0, j) for j in range(r.nclones)])
+            out[name] = {"fwd_s": t1 - t0, "bwd_s": t2 - t1, "J_mean": float(np.mean(J))}
+    errs = {"fp32": [], "fp64": []}
+    with clbm.Sampler(descs, clbm.FP64, max_steps=T) as f:
+        for _ in range(directions):
+            d = rng.normal(0.0, 1.0, base.size)
+            f.load_run(0, S0 + eps * d)
+            jp = f.drag_fwd(T, every)
+            f.load_run(0, S0 - eps * d)
+            jm = f.drag_fwd(T, every)
+            fd = (jp - jm) / (2 * eps)
+            for k in errs:
+                ad = (grads[k] * d).reshape(r.nclones, n).sum(axis=1)
+                errs[k].extend((np.abs(ad - fd) / np.abs(fd)).tolist())
+    for k in errs:
+        e = np.array(errs[k])
+        out[k].update({"rel_err_max": float(e.max()), "rel_err_median": float(np.median(e))})
+    lups = r.nclones * r.nodes * T
+    line = {"study": "adjoint", "workload": wl.name, "directions": directions, "fd_eps": eps,
+            "checkpoint_every": every, "perturbation_sigma": r.noise, "comparisons": len(errs["fp32"]),
+            "results": out, "fp32_fwd_bwd_clone_lups": lups / (out["fp32"]["fwd_s"] + out["fp32"]["bwd_s"])}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -243,7 +294,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--graph", action="store_true", help="replay each interval as a CUDA graph")
-    ap.add_argument("--study", choices=["precision"], default=None)
+    ap.add_argument("--study", choices=["precision", "adjoint"], default=None)
     args = ap.parse_args()
     from clbm import configs
     wl = configs.WORKLOADS[args.workload]()
@@ -253,6 +304,9 @@ def main():
         return
     if args.study == "precision":
         precision_study(args, wl)
+        return
+    if args.study == "adjoint":
+        adjoint_study(args, wl)
         return
 
     import torch

@@ -124,4 +124,11 @@ def c2_fp32() -> Workload:
     return c2(FP32)
 
 
-WORKLOADS = {"c1": c1, "c2": c2, "c2f32": c2_fp32, "c3": c3, "c3s": c3_small, "c3m": c3_medium, "c4": c4}
+def c5() -> Workload:
+    """Adjoint drag gradient: 64 clones of 400x100, square 20 at (100,50),
+    gradient of the drag integrated over T = 200 steps, checkpoints every 20."""
+    return Workload("c5_adjoint_64x400x100", [Run(400, 100, 20, 100, 50, 64, 0.05, 0.56, 0.0, 1e-4, 5)],
+                    200, 1, FP32)
+
+
+WORKLOADS = {"c5": c5, "c1": c1, "c2": c2, "c2f32": c2_fp32, "c3": c3, "c3s": c3_small, "c3m": c3_medium, "c4": c4}
