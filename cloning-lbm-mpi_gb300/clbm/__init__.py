@@ -31,7 +31,7 @@ EXPORTS = [
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
-    "clbm_set_pending_labels", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
+    "clbm_set_pending_labels", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -95,6 +95,8 @@ def lib() -> C.CDLL:
         L.clbm_intervals_done.argtypes = [vp, i, C.POINTER(i)]
         L.clbm_scgf.argtypes = [vp, i, i, i, d, C.POINTER(d)]
         L.clbm_set_pending_labels.argtypes = [vp, i, vp]
+        L.clbm_enable_history.argtypes = [vp, i]
+        L.clbm_reconstruct_lineages.argtypes = [vp, i, C.POINTER(i), vp, vp]
         L.clbm_drag_fwd.argtypes = [vp, i, i, vp]
         L.clbm_drag_bwd.argtypes = [vp]
         L.clbm_get_drag_grad_aos_f64.argtypes = [vp, i, i, vp]
@@ -268,6 +270,20 @@ class Sampler:
         out = C.c_double()
         check(lib().clbm_scgf(self.h, run, first, count, dT, C.byref(out)), "clbm_scgf")
         return out.value
+
+    def enable_history(self, max_intervals: int):
+        check(lib().clbm_enable_history(self.h, max_intervals), "clbm_enable_history")
+
+    def reconstruct(self, run: int, steps: int):
+        """(lineage drag series [nclones][n*steps], ancestors [nclones][n])"""
+        n = C.c_int()
+        check(lib().clbm_reconstruct_lineages(self.h, run, C.byref(n), None, None), "clbm_reconstruct_lineages")
+        nc = self.runs[run].nclones
+        out = np.empty((nc, n.value * steps))
+        anc = np.empty((nc, n.value), np.int32)
+        check(lib().clbm_reconstruct_lineages(self.h, run, C.byref(n), _p(out), _p(anc)),
+              "clbm_reconstruct_lineages")
+        return out, anc
 
     def drag_fwd(self, steps: int, every: int) -> np.ndarray:
         J = np.empty(sum(r.nclones for r in self.runs))

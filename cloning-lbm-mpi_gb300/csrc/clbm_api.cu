@@ -69,6 +69,11 @@ struct clbm_ctx {
   int total_tiles[3] = {0, 0, 0};
   int step_variant = 0;  // FP32 step launch variant (clbm_autotune)
   bool pending = false;  // a clone step's copies/perturbations await the next interval
+  // lineage history (clbm_enable_history)
+  double *hist_drag = nullptr;
+  int *hist_labels = nullptr;
+  int hist_max = 0, hist_steps = 0;
+  bool hist_steps_varied = false;
   int *d_zeros = nullptr;
   // adjoint: forward checkpoints of P every adj_every steps
   struct {
@@ -126,7 +131,8 @@ extern "C" int clbm_destroy(clbm_ctx *c) {
                   c->d.labels, c->d.mark, c->d.copies_pre, c->d.copies_post, c->d.prefactors,
                   c->d.pert, c->d.partials, c->d.scratch_i, c->d.scratch_d, c->d.snaps,
                   c->d.rvalues, c->d.logr, c->d.err, c->d.terms, c->d_identity, c->d_zeros,
-                  c->adj.s0, c->adj.ckpt, c->adj.seg, c->adj.sig[0], c->adj.sig[1]};
+                  c->adj.s0, c->adj.ckpt, c->adj.seg, c->adj.sig[0], c->adj.sig[1],
+                  c->hist_drag, c->hist_labels};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -437,6 +443,12 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
   }
   if (prof && (e = cudaEventRecord(e1, s)) != cudaSuccess) return e;
   if ((e = launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, s)) != cudaSuccess) return e;
+  if (c->hist_max > 0) {
+    if (c->hist_steps == 0) c->hist_steps = steps;
+    if (c->hist_steps != steps) c->hist_steps_varied = true;
+    if ((e = launch_hist_drag(c->d, c->total_clones, steps, c->hist_drag, c->hist_max, s)) != cudaSuccess)
+      return e;
+  }
   // the pending copies and perturbations have been applied
   if ((e = cudaMemcpyAsync(c->d.labels, c->d_identity, sizeof(int) * c->total_clones,
                            cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
@@ -468,6 +480,13 @@ extern "C" int clbm_run_interval(clbm_ctx *c, int steps) {
   return CLBM_OK;
 }
 
+static cudaError_t enqueue_clone(clbm_ctx *c) {
+  cudaError_t e = launch_clone(c->d, c->nruns, c->stream);
+  if (e == cudaSuccess && c->hist_max > 0)
+    e = launch_hist_labels(c->d, c->total_clones, c->hist_labels, c->hist_max, c->stream);
+  return e;
+}
+
 static int check_error_word(clbm_ctx *c) {
   unsigned w = 0;
   CK(cudaMemcpyAsync(&w, c->d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
@@ -483,7 +502,7 @@ static int check_error_word(clbm_ctx *c) {
 extern "C" int clbm_clone_step(clbm_ctx *c) {
   if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
   if (c->last_steps < 1) return fail(CLBM_ERR_INVALID, "clone step before any interval");
-  CK(launch_clone(c->d, c->nruns, c->stream));
+  CK(enqueue_clone(c));
   c->pending = true;
   return check_error_word(c);
 }
@@ -549,7 +568,7 @@ static int graph_for(clbm_ctx *c, int steps, int sbuf, cudaGraphExec_t *exec) {
   cudaGraph_t graph = nullptr;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = enqueue_interval(c, steps, sbuf);
-  if (e == cudaSuccess) e = launch_clone(c->d, c->nruns, c->stream);
+  if (e == cudaSuccess) e = enqueue_clone(c);
   cudaError_t e2 = cudaStreamEndCapture(c->stream, &graph);
   if (e == cudaSuccess) e = e2;
   if (e != cudaSuccess) {
@@ -588,7 +607,7 @@ extern "C" int clbm_run_sampler(clbm_ctx *c, int steps, int intervals, double *r
       CK(cudaGraphLaunch(ge, c->stream));
     } else {
       CK(enqueue_interval(c, steps, c->s_buf, c->profiling));
-      CK(launch_clone(c->d, c->nruns, c->stream));
+      CK(enqueue_clone(c));
     }
     c->s_buf = sbuf_after(c->s_buf, steps);
     c->last_steps = steps;
@@ -874,4 +893,59 @@ extern "C" int clbm_get_drag_grad_aos_f64(clbm_ctx *c, int run, int clone, doubl
   if (c->precision != CLBM_FP64)  // soa_to_aos adds back w[k] for states; a gradient has no shift
     for (size_t i = 0; i < n; i++) aos[i] -= w_of((int)(i % 9));
   return CLBM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Lineage reconstruction (post_processing/reconstruction.cpp:35-109 on the
+// device): keep every interval's drag series and labels, then trace each
+// final slot back through its ancestors.
+extern "C" int clbm_enable_history(clbm_ctx *c, int max_intervals) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  if (max_intervals < 1 || max_intervals > c->d.max_intervals) return fail(CLBM_ERR_INVALID, "max_intervals out of range");
+  if (c->hist_drag) cudaFree(c->hist_drag);
+  if (c->hist_labels) cudaFree(c->hist_labels);
+  c->hist_drag = nullptr;
+  c->hist_labels = nullptr;
+  c->hist_max = 0;
+  CK(cudaMalloc((void **)&c->hist_drag, sizeof(double) * (size_t)max_intervals * c->total_clones * c->max_steps));
+  CK(cudaMalloc((void **)&c->hist_labels, sizeof(int) * (size_t)max_intervals * c->total_clones));
+  c->hist_max = max_intervals;
+  c->hist_steps = 0;
+  c->hist_steps_varied = false;
+  destroy_graphs(c);
+  int done = 0;
+  CK(cudaMemcpyAsync(&done, &c->d.state[0].interval, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (done != 0) return fail(CLBM_ERR_INVALID, "enable the history before the first interval");
+  return CLBM_OK;
+}
+
+extern "C" int clbm_reconstruct_lineages(clbm_ctx *c, int run, int *nintervals, double *out,
+                                         int *ancestors) {
+  if (int st = check_run(c, run)) return st;
+  if (c->hist_max < 1) return fail(CLBM_ERR_INVALID, "history not enabled (clbm_enable_history)");
+  if (c->hist_steps_varied) return fail(CLBM_ERR_INVALID, "intervals of different lengths in the history");
+  int done = 0;
+  CK(cudaMemcpyAsync(&done, &c->d.state[0].interval, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const int n = std::min(done, c->hist_max);
+  if (nintervals) *nintervals = n;
+  if (n < 1 || (!out && !ancestors)) return CLBM_OK;
+  const RunDev &R = c->runs_h[run];
+  const int steps = c->hist_steps;
+  int *d_anc = nullptr;
+  double *d_out = nullptr;
+  CK(cudaMallocAsync((void **)&d_anc, sizeof(int) * (size_t)R.nclones * n, c->stream));
+  cudaError_t e = cudaMallocAsync((void **)&d_out, sizeof(double) * (size_t)R.nclones * n * steps, c->stream);
+  if (e == cudaSuccess)
+    e = launch_reconstruct(c->hist_drag, c->hist_labels, c->total_clones, R.clone_base, R.nclones, n, steps,
+                           c->max_steps, d_anc, d_out, c->stream);
+  if (e == cudaSuccess && out)
+    e = cudaMemcpyAsync(out, d_out, sizeof(double) * (size_t)R.nclones * n * steps, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && ancestors)
+    e = cudaMemcpyAsync(ancestors, d_anc, sizeof(int) * (size_t)R.nclones * n, cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(d_anc, c->stream);
+  if (d_out) cudaFreeAsync(d_out, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return clbm_status_from_cuda(e);
 }

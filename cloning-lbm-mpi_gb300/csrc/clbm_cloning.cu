@@ -343,6 +343,76 @@ cudaError_t launch_scgf(const double *logr, int first, int count, double dT, dou
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// History for lineage reconstruction: every interval's drag series and the
+// labels of the clone step that ends it, indexed by the device-side interval
+// counter so that graph replays record correctly.
+__global__ void k_hist_drag(DevArrays d, int total_clones, int steps, double *hist, int max_hist) {
+  const int t = d.state[0].interval;  // interval being finished (before its clone step)
+  if (t >= max_hist) return;
+  const long long n = (long long)total_clones * d.max_steps;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    hist[(long long)t * n + i] = d.drag[i];
+}
+
+__global__ void k_hist_labels(DevArrays d, int total_clones, int *hist, int max_hist) {
+  const int t = d.state[0].interval - 1;  // clone step just completed
+  if (t < 0 || t >= max_hist) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total_clones; i += gridDim.x * blockDim.x)
+    hist[(long long)t * total_clones + i] = d.labels[i];
+}
+
+cudaError_t launch_hist_drag(const DevArrays &d, int total_clones, int steps, double *hist, int max_hist,
+                             cudaStream_t s) {
+  k_hist_drag<<<592, 256, 0, s>>>(d, total_clones, steps, hist, max_hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hist_labels(const DevArrays &d, int total_clones, int *hist, int max_hist,
+                               cudaStream_t s) {
+  k_hist_labels<<<(total_clones + 255) / 256, 256, 0, s>>>(d, total_clones, hist, max_hist);
+  return cudaGetLastError();
+}
+
+// Ancestors of the final slots (post_processing/reconstruction.cpp:72-108
+// restated): slot_{n-1} = j, slot_t = labels_t[slot_{t+1}].
+__global__ void k_ancestors(const int *hist_labels, int total_clones, int clone_base, int nclones,
+                            int n, int *anc) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nclones) return;
+  int slot = j;
+  anc[(long long)j * n + (n - 1)] = slot;
+  for (int t = n - 2; t >= 0; t--) {
+    slot = hist_labels[(long long)t * total_clones + clone_base + slot];
+    anc[(long long)j * n + t] = slot;
+  }
+}
+
+// out[j][t*steps + s] = drag of slot anc[j][t] in interval t, step s
+__global__ void k_gather_lineages(const double *hist_drag, const int *anc, int total_clones,
+                                  int clone_base, int nclones, int n, int steps, int max_steps,
+                                  double *out) {
+  const long long total = (long long)nclones * n * steps;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int s = (int)(i % steps);
+    const long long q = i / steps;
+    const int t = (int)(q % n), j = (int)(q / n);
+    const int slot = anc[(long long)j * n + t];
+    out[i] = hist_drag[((long long)t * total_clones + clone_base + slot) * max_steps + s];
+  }
+}
+
+cudaError_t launch_reconstruct(const double *hist_drag, const int *hist_labels, int total_clones,
+                               int clone_base, int nclones, int n, int steps, int max_steps,
+                               int *anc, double *out, cudaStream_t s) {
+  k_ancestors<<<(nclones + 127) / 128, 128, 0, s>>>(hist_labels, total_clones, clone_base, nclones, n, anc);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_gather_lineages<<<1184, 256, 0, s>>>(hist_drag, anc, total_clones, clone_base, nclones, n, steps,
+                                         max_steps, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_clone(const DevArrays &d, int nruns, cudaStream_t s) {
   k_clone<<<nruns, CLONE_THREADS, 0, s>>>(d, nruns);
   return cudaGetLastError();

@@ -98,6 +98,13 @@ cudaError_t launch_adj_init(bool f64, const RunDev *runs, int nruns, const void 
 cudaError_t launch_adj_step(bool f64, const RunDev *runs, int nruns, const void *sigma_in,
                             void *sigma_out, const void *P, bool with_drag, bool from_s0,
                             int blocks, cudaStream_t s);
+cudaError_t launch_hist_drag(const DevArrays &d, int total_clones, int steps, double *hist, int max_hist,
+                             cudaStream_t s);
+cudaError_t launch_hist_labels(const DevArrays &d, int total_clones, int *hist, int max_hist,
+                               cudaStream_t s);
+cudaError_t launch_reconstruct(const double *hist_drag, const int *hist_labels, int total_clones,
+                               int clone_base, int nclones, int n, int steps, int max_steps,
+                               int *anc, double *out, cudaStream_t s);
 cudaError_t launch_scgf(const double *logr, int first, int count, double dT, double *out,
                         cudaStream_t s);
 cudaError_t launch_init_equilibrium(bool f64, const RunDev *runs, int nruns, int run, void *pop,

@@ -14,6 +14,10 @@
 //   --fp32           FP32 populations (default FP64, the reference's arithmetic)
 //   --no-zero-mean   drag without the AVG = 1.775 shift (the Makefile sets
 //                    ZERO_MEAN, so it is on by default)
+//   --reconstruct    (pops variant) also write every final slot's lineage
+//                    drag series to <parent>reconstructed/clone_<j>/data_force.datout,
+//                    what post_processing/reconstruction.cpp assembles
+//                    from labels.dat and the slot files
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -32,6 +36,7 @@ struct Opts {
   int ranks = 1;
   int precision = CLBM_FP64;
   bool zero_mean = true;
+  bool reconstruct = false;
   std::string input;
 };
 
@@ -45,6 +50,8 @@ Opts parse(int argc, char **argv) {
       o.precision = CLBM_FP32;
     else if (a == "--no-zero-mean")
       o.zero_mean = false;
+    else if (a == "--reconstruct")
+      o.reconstruct = true;
     else
       o.input = a;
   }
@@ -116,6 +123,7 @@ int run_pops(const Opts &o) {
   clbm_ctx *ctx = nullptr;
   int s = clbm_create(&d, 1, o.precision, st.steps2, 0, &ctx);
   if (s) return die(log, "clbm_create", s);
+  if (o.reconstruct && (s = clbm_enable_history(ctx, st.intervals))) return die(log, "history", s);
   if ((s = clbm_load_run_aos_f64(ctx, 0, states.data())) ||
       (s = clbm_set_snapshots_aos_f64(ctx, 0, NN, snaps.data())))
     return die(log, "loading states", s);
@@ -138,6 +146,18 @@ int run_pops(const Opts &o) {
     append_binary(labels_file, labels.data(), sizeof(int) * in.nc);
   }
   write_binary(in.parent + "rvalues.dat", rrec.data(), sizeof(double) * st.intervals);
+  if (o.reconstruct) {
+    int n = 0;
+    std::vector<double> lin((size_t)in.nc * st.intervals * st.steps2);
+    if ((s = clbm_reconstruct_lineages(ctx, 0, &n, lin.data(), nullptr))) return die(log, "reconstruction", s);
+    const std::string dir = in.parent + "reconstructed/";
+    make_dir(dir);
+    for (int j = 0; j < in.nc; j++) {
+      make_dir(clone_dir(dir, j));
+      write_binary(clone_dir(dir, j) + "data_force.datout", &lin[(size_t)j * n * st.steps2],
+                   sizeof(double) * (size_t)n * st.steps2);
+    }
+  }
   clbm_destroy(ctx);
   return 0;
 }

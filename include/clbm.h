@@ -240,6 +240,18 @@ int clbm_autotune(clbm_ctx *ctx, int launches, int *best,
                   double *ms_per_variant, int *nvariants);
 int clbm_set_step_variant(clbm_ctx *ctx, int variant);
 
+/* ---- lineage reconstruction (post_processing/reconstruction.cpp:35-109) ----
+ * clbm_enable_history(ctx, max_intervals), before the first interval, keeps
+ * every interval's drag series and the labels of its clone step on the
+ * device (max_intervals * clones * max_steps doubles).
+ * clbm_reconstruct_lineages then traces each final slot j back through its
+ * ancestors (slot_t = labels_t[slot_{t+1}]) and returns, for the n recorded
+ * intervals (*nintervals), out[j][t*steps + s] = drag of j's ancestor in
+ * interval t, step s, and ancestors[j][t] (either pointer may be NULL). */
+int clbm_enable_history(clbm_ctx *ctx, int max_intervals);
+int clbm_reconstruct_lineages(clbm_ctx *ctx, int run, int *nintervals,
+                              double *out, int *ancestors);
+
 /* ---- differentiation: adjoint of the interval-integrated drag ------------
  * J_j = dt * sum_{t<steps} (F_t*force_scale - force_shift) of every clone j
  * (the weight integral s_j of the sampler, pops driver :445-465), started

@@ -23,11 +23,14 @@ def drivers(gpu):
 
 @pytest.mark.parametrize("i", range(2))
 def test_pops_driver_files_match_reference(drivers, orc, tmp_path, i):
+    """Also --reconstruct: lineage files built from the driver's own labels.dat
+    and slot files (what post_processing/reconstruction.cpp does) must equal
+    the device-side reconstruction."""
     z = np.load(GOLD / "pops_driver.npz")
     L, Nc, U0, tau, alpha, eps, T, dT = z["params"][i]
     p = dict(L=int(L), Nc=int(Nc), U0=U0, tau=tau, alpha=alpha, eps=eps, T=T, dT=dT)
     stage_pops_run(orc, tmp_path, p)
-    r = subprocess.run([str(drivers / "TLGK_LBM_POPS_PERTURB"), "input"], cwd=tmp_path,
+    r = subprocess.run([str(drivers / "TLGK_LBM_POPS_PERTURB"), "--reconstruct", "input"], cwd=tmp_path,
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     out = tmp_path / "out"
@@ -40,6 +43,17 @@ def test_pops_driver_files_match_reference(drivers, orc, tmp_path, i):
         assert f.shape == g.shape
         assert np.array_equal(f[:steps], g[:steps])
         assert np.abs(f - g).max() <= 1e-12 * np.abs(g).max()
+    labels = np.fromfile(out / "labels.dat", np.int32).reshape(-1, int(Nc))
+    nint = labels.shape[0]
+    slots = [np.fromfile(out / f"clone_{j}" / "data_force.datout").reshape(nint, steps) for j in range(int(Nc))]
+    for j in range(int(Nc)):
+        slot, expect = j, []
+        for t in range(nint - 1, -1, -1):
+            expect.append(slots[slot][t])
+            if t > 0:
+                slot = labels[t - 1][slot]
+        lin = np.fromfile(out / "reconstructed" / f"clone_{j}" / "data_force.datout")
+        assert np.array_equal(lin, np.concatenate(expect[::-1]))
 
 
 def test_pops_driver_two_ranks_matches_oracle(drivers, orc, tmp_path):

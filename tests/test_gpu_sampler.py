@@ -231,3 +231,31 @@ def test_scgf_and_genealogy_lock(gpu, clbm_lib, orc):
         assert abs(psi - expect) <= 1e-13 * abs(expect)
         psi32 = b.scgf(0, dT)
         assert abs(psi32 - psi) <= 1e-4 * abs(psi)
+
+
+@pytest.mark.parametrize("flags", [0, 1])
+def test_lineage_reconstruction(gpu, clbm_lib, orc, flags):
+    """Each final slot's drag series traced back through its ancestors, as
+    post_processing/reconstruction.cpp assembles it from labels.dat and the
+    slot files, against the oracle's outputs."""
+    g, phys, T, n, nc, seed = channel_case(orc, k=6.0, n=5, T=20)
+    d = desc(clbm_lib, g, nc, perturb_mode=2, eps=1e-4, seed=seed, **phys)
+    states = np.concatenate([orc.init_equilibrium(g, 0.05, 1e-3, seed, 0, j) for j in range(nc)])
+    ref = orc.run_sampler(g, states, steps=T, intervals=n, perturb_mode=2, eps=1e-4, seed=seed, **phys)
+    anc_ref = np.zeros((nc, n), np.int32)
+    series = np.zeros((nc, n * T))
+    for j in range(nc):
+        slot = j
+        for t in range(n - 1, -1, -1):
+            anc_ref[j, t] = slot
+            series[j, t * T:(t + 1) * T] = ref["drag"][t, slot]
+            if t > 0:
+                slot = ref["labels"][t - 1, slot]
+    assert (anc_ref[:, 0] != np.arange(nc)).any()
+    with clbm_lib.Sampler([d], clbm_lib.FP64, max_steps=T, flags=flags) as s:
+        s.enable_history(16)
+        s.load_run(0, states)
+        s.run_sampler(T, n)
+        out, anc = s.reconstruct(0, T)
+    assert np.array_equal(anc, anc_ref)
+    assert np.array_equal(out, series)
