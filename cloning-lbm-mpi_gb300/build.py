@@ -68,26 +68,28 @@ DRIVER_VARIANTS = (("TLGK_LBM", "plain"), ("TLGK_LBM_POPS_PERTURB", "pops"))
 
 
 def build_drivers(verbose: bool = False) -> list[Path]:
-    """The three drop-in executables (TLGK_LBM, TLGK_LBM_FORCING,
-    TLGK_LBM_POPS_PERTURB), C++ host code over libclbm's C ABI."""
+    """The drop-in executables (TLGK_LBM, TLGK_LBM_POPS_PERTURB,
+    TLGK_LBM_FORCING, LBM_BODYFORCE), C++ host code over libclbm's C ABI."""
     outs = []
     srcs = sorted(DRIVERS.glob("*.cpp"))
     if not srcs:
         return outs
     headers = list(DRIVERS.glob("*.h")) + [REPO / "include" / "clbm.h"]
     lib = BUILD / "libclbm.so"
-    common = [s for s in srcs if s.stem != "tlgk_main"]
-    main = DRIVERS / "tlgk_main.cpp"
+    mains = {"tlgk_main", "lbm_bodyforce"}
+    common = [s for s in srcs if s.stem not in mains]
+    link = [f"-L{BUILD}", "-lclbm", "-Wl,-rpath,$ORIGIN", "-lm"]
     jobs = []
-    for name, variant in DRIVER_VARIANTS:
+    targets = [(name, DRIVERS / "tlgk_main.cpp", [f"-DCLBM_VARIANT_{variant.upper()}"])
+               for name, variant in DRIVER_VARIANTS]
+    targets.append(("LBM_BODYFORCE", DRIVERS / "lbm_bodyforce.cpp", []))
+    for name, main, defs in targets:
         exe = BUILD / name
         outs.append(exe)
         if _stale(exe, srcs + headers + [lib]):
-            jobs.append([CXX, "-std=c++17", "-O2", f"-DCLBM_VARIANT_{variant.upper()}",
-                         "-I", str(REPO / "include"), "-o", str(exe), str(main),
-                         *map(str, common), f"-L{BUILD}", "-lclbm",
-                         f"-Wl,-rpath,$ORIGIN", "-lm"])
-    with ThreadPoolExecutor(max_workers=3) as ex:
+            jobs.append([CXX, "-std=c++17", "-O2", *defs, "-I", str(REPO / "include"), "-o", str(exe),
+                         str(main), *map(str, common), *link])
+    with ThreadPoolExecutor(max_workers=4) as ex:
         list(ex.map(_run, jobs))
     if verbose:
         print("built drivers:", ", ".join(o.name for o in outs))

@@ -31,7 +31,7 @@ EXPORTS = [
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
-    "clbm_set_pending_labels", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
+    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -95,6 +95,7 @@ def lib() -> C.CDLL:
         L.clbm_intervals_done.argtypes = [vp, i, C.POINTER(i)]
         L.clbm_scgf.argtypes = [vp, i, i, i, d, C.POINTER(d)]
         L.clbm_set_pending_labels.argtypes = [vp, i, vp]
+        L.clbm_macro_fields.argtypes = [vp, i, i, vp, vp, vp]
         L.clbm_enable_history.argtypes = [vp, i]
         L.clbm_reconstruct_lineages.argtypes = [vp, i, C.POINTER(i), vp, vp]
         L.clbm_drag_fwd.argtypes = [vp, i, i, vp]
@@ -270,6 +271,12 @@ class Sampler:
         out = C.c_double()
         check(lib().clbm_scgf(self.h, run, first, count, dT, C.byref(out)), "clbm_scgf")
         return out.value
+
+    def macro(self, run: int, clone: int):
+        n = self.runs[run].width * self.runs[run].height
+        rho, ux, uy = np.empty(n), np.empty(n), np.empty(n)
+        check(lib().clbm_macro_fields(self.h, run, clone, _p(rho), _p(ux), _p(uy)), "clbm_macro_fields")
+        return rho, ux, uy
 
     def enable_history(self, max_intervals: int):
         check(lib().clbm_enable_history(self.h, max_intervals), "clbm_enable_history")

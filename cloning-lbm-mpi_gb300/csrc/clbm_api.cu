@@ -949,3 +949,21 @@ extern "C" int clbm_reconstruct_lineages(clbm_ctx *c, int run, int *nintervals, 
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return clbm_status_from_cuda(e);
 }
+
+extern "C" int clbm_macro_fields(clbm_ctx *c, int run, int clone, double *rho, double *ux, double *uy) {
+  if (int st = check_run(c, run)) return st;
+  const RunDev &R = c->runs_h[run];
+  if (clone < 0 || clone >= R.nclones || !rho || !ux || !uy) return fail(CLBM_ERR_INVALID, "bad clone or NULL array");
+  if (c->pending) return fail(CLBM_ERR_INVALID, "a clone step is pending; run an interval first");
+  const size_t n = R.nodes;
+  double *d = nullptr;
+  CK(cudaMallocAsync((void **)&d, 3 * n * sizeof(double), c->stream));
+  cudaError_t e = launch_macro(c->precision == CLBM_FP64, c->d.runs, run, clone, R.nodes, c->pop[c->s_buf], d,
+                               d + n, d + 2 * n, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rho, d, n * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ux, d + n, n * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(uy, d + 2 * n, n * 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(d, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return clbm_status_from_cuda(e);
+}

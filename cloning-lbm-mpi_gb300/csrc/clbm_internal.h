@@ -114,6 +114,8 @@ cudaError_t launch_aos_to_soa(bool f64, const RunDev *runs, int run, int clone0,
                               const double *aos, void *pop, cudaStream_t s);
 cudaError_t launch_soa_to_aos(bool f64, const RunDev *runs, int run, int clone, const void *pop,
                               double *aos, cudaStream_t s);
+cudaError_t launch_macro(bool f64, const RunDev *runs, int run, int clone, int nodes, const void *pop,
+                         double *rho, double *ux, double *uy, cudaStream_t s);
 cudaError_t launch_snaps_to_soa(const RunDev *runs, int run, int nsnap, const double *aos,
                                 double *snaps, cudaStream_t s);
 

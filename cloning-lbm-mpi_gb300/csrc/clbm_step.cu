@@ -542,6 +542,37 @@ __global__ void k_snaps_to_soa(const RunDev *runs, int run, const double *aos, d
   for (int k = 0; k < 9; k++) dst[k * R.plane] = src[k];
 }
 
+// Macroscopic fields of a clone's pre-collision state in the reference's node
+// order idx(x,y) = y + Dy*x: rho, the force-shifted ux = jx/rho + beta/(2 rho)
+// and uy, as streamCollCompute.cpp:21-28 computes them before colliding
+// (the fields write_fluid_vtk prints, write_vtk.cpp:38-49).
+template <bool F64>
+__global__ void k_macro(const RunDev *runs, int run, int clone, const void *popv, double *rho,
+                        double *ux, double *uy) {
+  using T = pop_t<F64>;
+  const RunDev &R = runs[run];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // t = y + H*x
+  if (t >= R.nodes) return;
+  const int x = t / R.H, y = t - x * R.H;
+  const T *src = (const T *)popv + R.pop_base + (long long)clone * 9 * R.plane + (long long)y * R.W + x;
+  double f[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) f[k] = F64 ? (double)src[k * R.plane] : w_of(k) + (double)src[k * R.plane];
+  const Moments64 m = moments_ref64(f);
+  rho[t] = m.rho;
+  ux[t] = DADD(DDIV(m.jx, m.rho), DDIV(DMUL(0.5, R.beta), m.rho));
+  uy[t] = DDIV(m.jy, m.rho);
+}
+
+cudaError_t launch_macro(bool f64, const RunDev *runs, int run, int clone, int nodes, const void *pop,
+                         double *rho, double *ux, double *uy, cudaStream_t s) {
+  if (f64)
+    k_macro<true><<<(nodes + 255) / 256, 256, 0, s>>>(runs, run, clone, pop, rho, ux, uy);
+  else
+    k_macro<false><<<(nodes + 255) / 256, 256, 0, s>>>(runs, run, clone, pop, rho, ux, uy);
+  return cudaGetLastError();
+}
+
 static cudaError_t run_geometry(const RunDev *runs, int run, RunDev &h, cudaStream_t s) {
   cudaError_t e = cudaMemcpyAsync(&h, runs + run, sizeof(RunDev), cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return e;

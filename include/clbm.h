@@ -240,6 +240,13 @@ int clbm_autotune(clbm_ctx *ctx, int launches, int *best,
                   double *ms_per_variant, int *nvariants);
 int clbm_set_step_variant(clbm_ctx *ctx, int variant);
 
+/* Macroscopic fields of a clone's current pre-collision state, HOST arrays of
+ * Dx*Dy values in the reference's node order y + Dy*x: rho, ux (shifted by
+ * beta/(2 rho), as streamCollCompute.cpp:28 computes it) and uy -- what
+ * write_fluid_vtk prints (src/lbm_src/write_vtk.cpp:8-53). */
+int clbm_macro_fields(clbm_ctx *ctx, int run, int clone, double *rho,
+                      double *ux, double *uy);
+
 /* ---- lineage reconstruction (post_processing/reconstruction.cpp:35-109) ----
  * clbm_enable_history(ctx, max_intervals), before the first interval, keeps
  * every interval's drag series and the labels of its clone step on the

@@ -94,3 +94,39 @@ def test_plain_driver(drivers, orc, tmp_path):
                           alpha=0.04, force_scale=1.0, force_shift=0.0, dt=1.0 / t0)
     assert np.array_equal(np.fromfile(tmp_path / "labels.dat", np.int32), ref["labels"].ravel())
     np.testing.assert_allclose(np.fromfile(tmp_path / "rvalues.dat"), ref["rvalues"], rtol=1e-13)
+
+
+def test_bodyforce_warmup_and_snapshots(drivers, orc, tmp_path):
+    """LBM_BODYFORCE (main_bodyforce.cpp) from the rest state: final
+    populations, raw force every facquForce steps and the ux probe every
+    facquU steps against the oracle; snapshot mode writes popfiles and
+    popfiles_list.dat that TLGK_LBM_POPS_PERTURB reads."""
+    L, steps, tau, Ma = 4, 30, 0.6, 0.15
+    (tmp_path / "input.datin").write_text(f"1 {steps} {L} {tau} {Ma} run 0 10 3 5\n")
+    r = subprocess.run([str(drivers / "LBM_BODYFORCE"), "--snapshots", "3", "--every", "5"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    import math
+    g = orc.reference_square_geom(L)
+    Dy = 4 * L + 1
+    cs = 1.0 / math.sqrt(3)
+    beta = 8 * (1.0 / 3 * (tau - 0.5)) * (cs * cs * Ma) / ((Dy - 1) // 2) / ((Dy - 1) // 2)
+    f = np.tile(orc.W, Dy * Dy)
+    force, ux = [], []
+    for t in range(steps + 15):
+        f_new, _, rho, uxf, uyf = orc.lbm_step(g, f, beta, tau)
+        if t < steps and t % 5 == 0:
+            ux.append(uxf[(Dy // 4) + Dy * (Dy // 4)])
+        F = orc.force(g, f_new, 1.0 / tau)
+        if t < steps and t % 3 == 0:
+            force.append(F)
+        f = f_new
+        if t == steps - 1:
+            assert np.array_equal(np.fromfile(tmp_path / "run" / "pops.datout"), f)
+        if t >= steps and (t + 1 - steps) % 5 == 0:
+            k = (t + 1 - steps) // 5 - 1
+            assert np.array_equal(np.fromfile(tmp_path / "run" / f"pops_{k}.datout"), f)
+    assert np.array_equal(np.fromfile(tmp_path / "run" / "data_force.datout"), np.array(force))
+    assert np.array_equal(np.fromfile(tmp_path / "run" / "ux_t.datout"), np.array(ux))
+    assert len(list((tmp_path / "run" / "vtk_fluid").glob("fluid_t*.vtk"))) == 3
+    assert (tmp_path / "run" / "popfiles_list.dat").read_text().split() == [f"pops_{k}.datout" for k in range(3)]
