@@ -64,7 +64,8 @@ def build_library(verbose: bool = False) -> Path:
     return lib
 
 
-DRIVER_VARIANTS = (("TLGK_LBM", "plain"), ("TLGK_LBM_POPS_PERTURB", "pops"))
+DRIVER_VARIANTS = (("TLGK_LBM", "plain"), ("TLGK_LBM_POPS_PERTURB", "pops"),
+                   ("TLGK_LBM_FORCING", "forcing"))
 
 
 def build_drivers(verbose: bool = False) -> list[Path]:

@@ -31,7 +31,7 @@ EXPORTS = [
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
-    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
+    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -49,6 +49,8 @@ class RunDesc(C.Structure):
         ("force_scale", C.c_double), ("force_shift", C.c_double), ("dt", C.c_double),
         ("perturb_mode", C.c_int), ("resample_mode", C.c_int),
         ("eps", C.c_double), ("seed", C.c_ulonglong), ("nsnap", C.c_int), ("reserved", C.c_int),
+        ("field_mode", C.c_int), ("field_steps", C.c_int), ("field_eps", C.c_double),
+        ("field_sigma", C.c_double),
     ]
 
 
@@ -96,6 +98,7 @@ def lib() -> C.CDLL:
         L.clbm_scgf.argtypes = [vp, i, i, i, d, C.POINTER(d)]
         L.clbm_set_pending_labels.argtypes = [vp, i, vp]
         L.clbm_macro_fields.argtypes = [vp, i, i, vp, vp, vp]
+        L.clbm_get_field_map.argtypes = [vp, i, i, vp, C.POINTER(i)]
         L.clbm_enable_history.argtypes = [vp, i]
         L.clbm_reconstruct_lineages.argtypes = [vp, i, C.POINTER(i), vp, vp]
         L.clbm_drag_fwd.argtypes = [vp, i, i, vp]
@@ -277,6 +280,14 @@ class Sampler:
         rho, ux, uy = np.empty(n), np.empty(n), np.empty(n)
         check(lib().clbm_macro_fields(self.h, run, clone, _p(rho), _p(ux), _p(uy)), "clbm_macro_fields")
         return rho, ux, uy
+
+    def field_map(self, run: int, clone: int):
+        """(map in the reference order y + H*x, clamped negative eigenvalues)"""
+        r = self.runs[run]
+        out = np.empty(r.width * r.height)
+        neg = C.c_int()
+        check(lib().clbm_get_field_map(self.h, run, clone, _p(out), C.byref(neg)), "clbm_get_field_map")
+        return out, neg.value
 
     def enable_history(self, max_intervals: int):
         check(lib().clbm_enable_history(self.h, max_intervals), "clbm_enable_history")

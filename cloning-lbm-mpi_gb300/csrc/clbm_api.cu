@@ -69,6 +69,12 @@ struct clbm_ctx {
   int total_tiles[3] = {0, 0, 0};
   int step_variant = 0;  // FP32 step launch variant (clbm_autotune)
   bool pending = false;  // a clone step's copies/perturbations await the next interval
+  // random body-force fields (forcing variant)
+  bool any_field = false;
+  float *d_spec = nullptr, *d_maps = nullptr;
+  float2 *d_tw = nullptr, *d_ybuf = nullptr;
+  int field_max_w = 0, field_max_m1 = 0, field_max_m2 = 0, field_max_tiles2 = 0;
+  std::vector<int> field_negative;  // spectrum entries below -1e-15 (clamped to 0)
   // lineage history (clbm_enable_history)
   double *hist_drag = nullptr;
   int *hist_labels = nullptr;
@@ -132,7 +138,7 @@ extern "C" int clbm_destroy(clbm_ctx *c) {
                   c->d.pert, c->d.partials, c->d.scratch_i, c->d.scratch_d, c->d.snaps,
                   c->d.rvalues, c->d.logr, c->d.err, c->d.terms, c->d_identity, c->d_zeros,
                   c->adj.s0, c->adj.ckpt, c->adj.seg, c->adj.sig[0], c->adj.sig[1],
-                  c->hist_drag, c->hist_labels};
+                  c->hist_drag, c->hist_labels, c->d_spec, c->d_maps, c->d_tw, c->d_ybuf};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -165,6 +171,9 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
     if (d.perturb_mode == CLBM_PERTURB_MIX && (d.nsnap < 1 || d.nsnap > MAX_SNAP))
       return fail(CLBM_ERR_INVALID, "snapshot mix needs 1 <= nsnap <= 64");
     if (!(d.tau > 0.5)) return fail(CLBM_ERR_INVALID, "tau must exceed 1/2");
+    if (d.field_mode < 0 || d.field_mode > 1) return fail(CLBM_ERR_INVALID, "unknown field_mode");
+    if (d.field_mode && (d.width > 1024 || d.height > 1024 || d.field_steps < 0))
+      return fail(CLBM_ERR_INVALID, "random field needs W, H <= 1024 and field_steps >= 0");
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
@@ -180,7 +189,10 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
   c->desc.assign(runs, runs + nruns);
   c->snaps_loaded.assign(nruns, 0);
   c->runs_h.resize(nruns);
-  long long pop = 0, terms = 0, snaps = 0;
+  long long pop = 0, terms = 0, snaps = 0, spec = 0, tw = 0, ybuf = 0, maps = 0;
+  std::vector<float> h_spec;
+  std::vector<float2> h_tw;
+  c->field_negative.assign(nruns, 0);
   int clones = 0, blocks = 0;
   for (int r = 0; r < nruns; r++) {
     const clbm_run_desc &d = runs[r];
@@ -237,6 +249,60 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
     R.nsnap = d.perturb_mode == CLBM_PERTURB_MIX ? d.nsnap : 0;
     R.seed = d.seed;
     R.run_id = (unsigned)r;
+    if (d.field_mode) {
+      // circulant embedding of exp(-r^2/(2 sigma^2)) on (2W-1) x (2H-1): the
+      // spectrum is separable, lambda[a][b] = l1[a] l2[b] / (M1 M2), l = DFT
+      // of the 1-D embedded Gaussian g[j] = exp(-min(j, M-j)^2 / (2 sigma^2))
+      const double sig = d.field_sigma > 0 ? d.field_sigma : 32.0;
+      const int M1 = 2 * d.width - 1, M2 = 2 * d.height - 1;
+      auto spectrum = [&](int M) {
+        std::vector<double> g(M), l(M), cs(M);
+        for (int j = 0; j < M; j++) {
+          const double dd = std::min(j, M - j);
+          g[j] = std::exp(-dd * dd / (2 * sig * sig));
+          cs[j] = std::cos(2.0 * M_PI * j / M);
+        }
+        for (int a = 0; a < M; a++) {
+          double acc = 0.0;
+          for (int j = 0; j < M; j++) acc += g[j] * cs[(int)(((long long)a * j) % M)];
+          l[a] = acc;
+        }
+        return l;
+      };
+      const std::vector<double> l1 = spectrum(M1), l2 = spectrum(M2);
+      R.field_mode = 1;
+      R.field_steps = d.field_steps;
+      R.M1 = M1;
+      R.M2 = M2;
+      R.field_eps = d.field_eps;
+      R.f_field_eps = (float)d.field_eps;
+      R.spec_base = spec;
+      R.tw1_base = tw;
+      R.tw2_base = tw + M1;
+      R.y_base = ybuf;
+      R.map_base = maps;
+      h_spec.resize(spec + (size_t)M1 * M2);
+      for (int a = 0; a < M1; a++)
+        for (int b = 0; b < M2; b++) {
+          const double lam = l1[a] * l2[b] / ((double)M1 * M2);
+          if (lam < -1e-15) c->field_negative[r]++;
+          h_spec[spec + (size_t)a * M2 + b] = lam > 0 ? (float)std::sqrt(lam) : 0.f;
+        }
+      h_tw.resize(tw + M1 + M2);
+      for (int k = 0; k < M1; k++)
+        h_tw[tw + k] = make_float2((float)std::cos(2.0 * M_PI * k / M1), (float)-std::sin(2.0 * M_PI * k / M1));
+      for (int k = 0; k < M2; k++)
+        h_tw[tw + M1 + k] = make_float2((float)std::cos(2.0 * M_PI * k / M2), (float)-std::sin(2.0 * M_PI * k / M2));
+      spec += (long long)M1 * M2;
+      tw += M1 + M2;
+      ybuf += (long long)d.nclones * d.width * M2;
+      maps += (long long)d.nclones * R.nodes;
+      c->any_field = true;
+      c->field_max_w = std::max(c->field_max_w, d.width);
+      c->field_max_m1 = std::max(c->field_max_m1, M1);
+      c->field_max_m2 = std::max(c->field_max_m2, M2);
+      c->field_max_tiles2 = std::max(c->field_max_tiles2, ((d.width + 15) / 16) * ((d.height + 15) / 16));
+    }
     pop += (long long)d.nclones * 9 * R.plane;
     terms += (long long)R.nterms * d.nclones;
     if (d.perturb_mode == CLBM_PERTURB_MIX) {
@@ -289,6 +355,15 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
   if ((e = cudaMalloc(&D.terms, (size_t)terms * max_steps * c->elem_size)) != cudaSuccess) return bail(e);
   if ((e = dalloc(c->d_identity, clones)) != cudaSuccess) return bail(e);
   if ((e = dalloc(c->d_zeros, clones)) != cudaSuccess) return bail(e);
+  if (c->any_field) {
+    if ((e = dalloc(c->d_spec, (size_t)spec)) != cudaSuccess) return bail(e);
+    if ((e = dalloc(c->d_tw, (size_t)tw)) != cudaSuccess) return bail(e);
+    if ((e = dalloc(c->d_ybuf, (size_t)ybuf)) != cudaSuccess) return bail(e);
+    if ((e = dalloc(c->d_maps, (size_t)maps)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemcpy(c->d_spec, h_spec.data(), sizeof(float) * spec, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemcpy(c->d_tw, h_tw.data(), sizeof(float2) * tw, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemset(c->d_maps, 0, sizeof(float) * maps)) != cudaSuccess) return bail(e);
+  }
   if ((e = cudaMemset(c->d_zeros, 0, sizeof(int) * clones)) != cudaSuccess) return bail(e);
 
   std::vector<RunState> st(nruns);
@@ -414,8 +489,14 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
                              c->d.snaps, c->d.partials, c->d.pert, c->total_blocks, c->total_clones, s);
     if (e != cudaSuccess) return e;
   }
+  if (c->any_field) {
+    FieldArgs fa{c->d.runs, c->nruns, c->d.state, c->d_spec, c->d_tw, c->d_ybuf, c->d_maps};
+    e = launch_fields(fa, c->total_clones, c->field_max_w, c->field_max_m1, c->field_max_m2,
+                      c->field_max_tiles2, s);
+    if (e != cudaSuccess) return e;
+  }
   ReseedArgs ra{c->d.runs, c->nruns, S, c->pop[1 - sbuf], c->d.labels, c->d.mark, c->d.pert,
-                c->d.prefactors, c->d.snaps, c->d.state, c->d.err};
+                c->d.prefactors, c->d.snaps, c->d.state, c->d.err, c->d_maps};
   if ((e = launch_reseed(f64, ra, c->total_blocks, s)) != cudaSuccess) return e;
   int cur = 1 - sbuf;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -436,7 +517,7 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
   for (int t = 0; t < steps; t++) {
     StepArgs a{c->d.runs, c->nruns, t, c->pop[cur], c->pop[1 - cur], c->d.terms, c->d.term_slab,
                c->d.err, c->total_clones, c->max_nodes,
-               {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}};
+               {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}, c->d_maps};
     if ((e = launch_step(f64, t == steps - 1, a, c->total_blocks, s, c->step_variant)) != cudaSuccess)
       return e;
     cur = 1 - cur;
@@ -966,4 +1047,20 @@ extern "C" int clbm_macro_fields(clbm_ctx *c, int run, int clone, double *rho, d
   cudaFreeAsync(d, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return clbm_status_from_cuda(e);
+}
+
+extern "C" int clbm_get_field_map(clbm_ctx *c, int run, int clone, double *map, int *negative) {
+  if (int st = check_run(c, run)) return st;
+  const RunDev &R = c->runs_h[run];
+  if (!R.field_mode) return fail(CLBM_ERR_INVALID, "run has no random field");
+  if (clone < 0 || clone >= R.nclones) return fail(CLBM_ERR_INVALID, "bad clone");
+  if (negative) *negative = c->field_negative[run];
+  if (!map) return CLBM_OK;
+  std::vector<float> f(R.nodes);
+  CK(cudaMemcpyAsync(f.data(), c->d_maps + R.map_base + (size_t)clone * R.nodes, sizeof(float) * R.nodes,
+                     cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int x = 0; x < R.W; x++)
+    for (int y = 0; y < R.H; y++) map[y + (size_t)R.H * x] = (double)f[(size_t)y * R.W + x];
+  return CLBM_OK;
 }

@@ -64,6 +64,15 @@ struct RunDev {
   unsigned long long seed;
   unsigned run_id;
   int pad2_;
+  // Gaussian random body-force field (forcing variant)
+  int field_mode, field_steps;
+  int M1, M2;                  // embedding sizes 2W-1, 2H-1
+  double field_eps;
+  float f_field_eps, f_pad2;
+  long long map_base;          // element offset of clone 0's map (W*H floats per clone)
+  long long spec_base;         // offset of the sqrt-spectrum (M1*M2 floats)
+  long long tw1_base, tw2_base;// offsets of the twiddle tables (complex floats)
+  long long y_base;            // offset of the stage-1 buffer (W*M2 complex per clone)
 };
 
 // Bounce-back classification of node (x,y): bit k set means the outgoing
@@ -115,7 +124,7 @@ __host__ __device__ inline double philox_uniform(unsigned long long seed, uint32
 }
 
 // Philox counter domains (top bits of the fourth word, run id below).
-enum : uint32_t { DOM_INIT = 1u, DOM_PERTURB = 2u, DOM_SYSTEMATIC = 3u };
+enum : uint32_t { DOM_INIT = 1u, DOM_PERTURB = 2u, DOM_SYSTEMATIC = 3u, DOM_FIELD = 4u };
 
 // ---- drand48 (POSIX 48-bit LCG), with jump-ahead ----------------------------
 constexpr uint64_t D48_A = 0x5DEECE66DULL, D48_C = 0xBULL, D48_MASK = (1ULL << 48) - 1;

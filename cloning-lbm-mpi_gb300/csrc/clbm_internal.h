@@ -52,6 +52,16 @@ struct DevArrays {
   int max_intervals;
 };
 
+struct FieldArgs {
+  const RunDev *runs;
+  int nruns;
+  const RunState *state;   // interval counter (random-stream counter)
+  const float *spec;       // sqrt spectra, [M1][M2] per field run
+  const float2 *twiddles;  // exp(-2 pi i k / M1), exp(-2 pi i k / M2) per field run
+  float2 *ybuf;            // stage-1 results, [W][M2] per clone
+  float *maps;             // fields, W*H per clone, node order y*W + x
+};
+
 struct StepArgs {
   const RunDev *runs;
   int nruns;
@@ -64,6 +74,7 @@ struct StepArgs {
   int total_clones;
   int max_nodes;
   int total_tiles[3]; // FP32 step grid for tiles of 128 / 256 / 512 nodes
+  const float *maps;  // random body-force fields (nullable)
 };
 
 struct ReseedArgs {
@@ -78,6 +89,7 @@ struct ReseedArgs {
   const double *snaps;
   const RunState *state;    // interval counter
   unsigned *err;
+  const float *maps;        // random body-force fields (nullable)
 };
 
 // kernel launchers (clbm_step.cu, clbm_cloning.cu)
@@ -105,6 +117,8 @@ cudaError_t launch_hist_labels(const DevArrays &d, int total_clones, int *hist, 
 cudaError_t launch_reconstruct(const double *hist_drag, const int *hist_labels, int total_clones,
                                int clone_base, int nclones, int n, int steps, int max_steps,
                                int *anc, double *out, cudaStream_t s);
+cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int max_m1, int max_m2,
+                          int max_tiles2, cudaStream_t s);
 cudaError_t launch_scgf(const double *logr, int first, int count, double dT, double *out,
                         cudaStream_t s);
 cudaError_t launch_init_equilibrium(bool f64, const RunDev *runs, int nruns, int run, void *pop,

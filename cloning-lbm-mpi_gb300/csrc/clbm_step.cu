@@ -84,14 +84,30 @@ __device__ __forceinline__ void store_drag_terms(const RunDev &R, const pop_t<F6
   if (y == R.ymin) T[(long long)(2 * (sy + 1) + sx + 1 + x - R.xmin) * nc + clone] = south;
 }
 
+// map: the node's random-field value when the collision is under the
+// spatial force, beta(x,y) = (1 + eps*map)*beta0 (streamCollCompute.cpp:63)
 template <bool F64>
 __device__ __forceinline__ void collide_node(const RunDev &R, const pop_t<F64> S[9],
-                                             pop_t<F64> P[9]) {
+                                             pop_t<F64> P[9], const float *map = nullptr) {
   if constexpr (F64) {
-    collide_ref64(S, P, R.beta, R.wcb, R.omega, R.om1);
+    if (map) {
+      const double beta = DMUL(DADD(1.0, DMUL(R.field_eps, (double)*map)), R.beta);
+      double wcb[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) wcb[k] = DMUL(DMUL(w_of(k), R.cforce), beta);
+      collide_ref64(S, P, beta, wcb, R.omega, R.om1);
+    } else {
+      collide_ref64(S, P, R.beta, R.wcb, R.omega, R.om1);
+    }
   } else {
-    collide_f32(S, P, R.f_beta, R.f_omega, R.f_cforce);
+    const float beta = map ? R.f_beta * (1.0f + R.f_field_eps * *map) : R.f_beta;
+    collide_f32(S, P, beta, R.f_omega, R.f_cforce);
   }
+}
+
+__device__ __forceinline__ const float *node_map(const float *maps, const RunDev &R, int clone, int n,
+                                                 bool on) {
+  return (on && maps) ? maps + R.map_base + (long long)clone * R.nodes + n : nullptr;
 }
 
 template <bool F64>
@@ -154,7 +170,7 @@ __global__ void __launch_bounds__(STEP_BLOCK) k_step(StepArgs a) {
     for (int k = 0; k < 9; k++) dst[k * plane + n] = S[k];
   } else {
     T P[9];
-    collide_node<F64>(R, S, P);
+    collide_node<F64>(R, S, P, node_map(a.maps, R, L.clone, n, R.field_mode && a.step + 1 < R.field_steps));
 #pragma unroll
     for (int k = 0; k < 9; k++) dst[k * plane + n] = P[k];
   }
@@ -235,7 +251,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_step_f32(StepArgs a) {
       drho += S[k];
     }
   } else {
-    drho = collide_f32_pairs(S, P, R.f_beta, R.f_omega, R.f_cforce);
+    float beta = R.f_beta;
+    if (R.field_mode && a.step + 1 < R.field_steps && a.maps)
+      beta *= 1.0f + R.f_field_eps * a.maps[R.map_base + (long long)clone * R.nodes + n];
+    drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
   }
   if (!(drho > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
 #pragma unroll
@@ -336,7 +355,7 @@ __global__ void __launch_bounds__(STEP_BLOCK) k_reseed(ReseedArgs a) {
     }
   }
   T P[9];
-  collide_node<F64>(R, S, P);
+  collide_node<F64>(R, S, P, node_map(a.maps, R, L.clone, n, R.field_mode && R.field_steps > 0));
 #pragma unroll
   for (int k = 0; k < 9; k++) dst[k * plane + n] = P[k];
 }

@@ -12,6 +12,7 @@
 // before the input file:
 //   --ranks P        reproduce the random streams of an `mpirun -n P` run
 //   --fp32           FP32 populations (default FP64, the reference's arithmetic)
+//   --seed S         (forcing variant) seed of the random-field stream
 //   --no-zero-mean   drag without the AVG = 1.775 shift (the Makefile sets
 //                    ZERO_MEAN, so it is on by default)
 //   --reconstruct    (pops variant) also write every final slot's lineage
@@ -37,6 +38,7 @@ struct Opts {
   int precision = CLBM_FP64;
   bool zero_mean = true;
   bool reconstruct = false;
+  unsigned long long seed = 1;
   std::string input;
 };
 
@@ -52,6 +54,8 @@ Opts parse(int argc, char **argv) {
       o.zero_mean = false;
     else if (a == "--reconstruct")
       o.reconstruct = true;
+    else if (a == "--seed" && i + 1 < argc)
+      o.seed = std::strtoull(argv[++i], nullptr, 10);
     else
       o.input = a;
   }
@@ -162,6 +166,92 @@ int run_pops(const Opts &o) {
   return 0;
 }
 
+// Forcing driver (src/mpi_LBM_GK_forcing.cpp): every clone draws a Gaussian
+// random field at the start of each interval and runs lbmTimeSteps1 steps
+// under beta(x,y) = (1 + eps map(x,y)) beta0, then lbmTimeSteps2 plain steps
+// (:333-395); no ZERO_MEAN shift, no perturbation of copies.  Outputs:
+// clone_<j>/evolution_<t>_clone_<j> (F/F0 every step), weights_evolution_<t>
+// (Nc doubles), copies_evolution_<t> (Nc int32 drawn, Nc int32 corrected),
+// rvalues.dat.  The fields come from a counter-based stream instead of
+// rand() (--seed S), so they are statistically, not bitwise, the reference's.
+int run_forcing(const Opts &o) {
+  Log log("output_TLGK.out");
+  Input in = read_input_forcing(o.input);
+  if (!in.ok) return die(log, "COULD NOT OPEN INPUT FILE " + o.input, 0);
+  const Setup st = setup_from(in, true);
+  if (o.ranks < 1 || in.nc % o.ranks) return die(log, "Nc must be a multiple of --ranks", 0);
+  const int T = st.steps1 + st.steps2;
+  if (T < 1 || st.intervals < 1 || st.steps1 < 0 || st.steps2 < 0)
+    return die(log, "no LB step or no cloning step to run", 0);
+  log.line("READ input file");
+  log.line("  Nc = " + std::to_string(in.nc) + " L = " + std::to_string(in.L) + " Dx = " + std::to_string(st.Dx));
+  make_dir(in.parent);
+  for (int j = 0; j < in.nc; j++) make_dir(in.parent + "clone_" + std::to_string(j));
+  const size_t n = 9 * (size_t)st.Dx * st.Dy;
+  std::vector<std::string> names;
+  if (!read_list(in.path + "popfiles_list.dat", names, in.nc))
+    return die(log, "COULD NOT OPEN INDEX FILE " + in.path + "popfiles_list.dat", 0);
+  const int local = in.nc / o.ranks;
+  std::vector<double> states(n * in.nc);
+  for (int j = 0; j < in.nc; j++) {
+    const int name_idx = (j >= local) ? j - local : in.nc - local + j;
+    if (!read_pops(in.path + names[name_idx], states, n, n * j))
+      return die(log, "could not read popfile " + names[name_idx], 0);
+  }
+  clbm_run_desc d{};
+  d.width = st.Dx;
+  d.height = st.Dy;
+  d.xmin = st.xmin;
+  d.xmax = st.xmax;
+  d.ymin = st.ymin;
+  d.ymax = st.ymax;
+  d.nclones = in.nc;
+  d.ranks = o.ranks;
+  d.tau = in.tau;
+  d.beta = st.beta0;
+  d.alpha = in.alpha;
+  d.force_scale = st.oneOvF0;
+  d.force_shift = 0.0;
+  d.dt = st.delta_t;
+  d.perturb_mode = CLBM_PERTURB_NONE;
+  d.resample_mode = CLBM_RESAMPLE_REFERENCE;
+  d.seed = o.seed;
+  d.field_mode = 1;
+  d.field_steps = st.steps1;
+  d.field_eps = in.eps;
+  d.field_sigma = 32.0;
+  clbm_ctx *ctx = nullptr;
+  int s = clbm_create(&d, 1, o.precision, T, 0, &ctx);
+  if (s) return die(log, "clbm_create", s);
+  if ((s = clbm_load_run_aos_f64(ctx, 0, states.data()))) return die(log, "loading states", s);
+  std::vector<double> drag((size_t)in.nc * T), rrec(st.intervals), w(in.nc);
+  std::vector<int> pre(in.nc), post(in.nc);
+  for (int t = 0; t < st.intervals; t++) {
+    log.line("    This is cloning step " + std::to_string(t));
+    if ((s = clbm_run_interval(ctx, T)) || (s = clbm_get_drag(ctx, 0, drag.data())))
+      return die(log, "interval", s);
+    if (t == 0) {
+      int neg = 0;
+      clbm_get_field_map(ctx, 0, 0, nullptr, &neg);
+      if (neg) log.line("  random field: " + std::to_string(neg) + " negative embedding eigenvalues set to 0");
+    }
+    for (int j = 0; j < in.nc; j++)
+      write_binary(in.parent + "clone_" + std::to_string(j) + "/evolution_" + std::to_string(t) + "_clone_" +
+                       std::to_string(j),
+                   &drag[(size_t)j * T], sizeof(double) * T);
+    if ((s = clbm_clone_step(ctx)) ||
+        (s = clbm_get_clone_result(ctx, 0, nullptr, &rrec[t], w.data(), pre.data(), post.data())))
+      return die(log, "cloning step", s);
+    write_binary(in.parent + "weights_evolution_" + std::to_string(t), w.data(), sizeof(double) * in.nc);
+    std::vector<int> cp(pre);
+    cp.insert(cp.end(), post.begin(), post.end());
+    write_binary(in.parent + "copies_evolution_" + std::to_string(t), cp.data(), sizeof(int) * cp.size());
+  }
+  write_binary(in.parent + "rvalues.dat", rrec.data(), sizeof(double) * st.intervals);
+  clbm_destroy(ctx);
+  return 0;
+}
+
 // Plain driver (src/mpi_LBM_GK.cpp): hard-coded Nc = 2, T = dT = 1,
 // alpha = 0.04 (:39-41, :61), parameters L tau Ma t0 from input_LBM.datin
 // (:48-53), every clone starting from one control-run state (:133-149), drag
@@ -244,6 +334,10 @@ int main(int argc, char **argv) {
 #elif defined(CLBM_VARIANT_PLAIN)
   return run_plain(o);
 #else
+  if (o.input.empty()) {
+    std::fprintf(stderr, "usage: TLGK_LBM_FORCING [--ranks P] [--fp32] [--seed S] inputfile\n");
+    return 2;
+  }
   return run_forcing(o);
 #endif
 }

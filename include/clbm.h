@@ -94,6 +94,17 @@ typedef struct {
   unsigned long long seed;    /* counter-based random streams */
   int nsnap;                  /* snapshots for CLBM_PERTURB_MIX (<= 64) */
   int reserved;
+  /* spatially random body force of the forcing variant
+   * (src/mpi_LBM_GK_forcing.cpp:333-364): at the start of every interval
+   * each clone draws a Gaussian random field `map` with covariance
+   * exp(-r^2 / (2 field_sigma^2)) (circulant embedding,
+   * src/perturbation_routines/generate_random_field.cpp:9-181, generalised
+   * from the reference's square domain to W x H), and its first field_steps
+   * steps use beta(x,y) = (1 + field_eps * map(x,y)) * beta. */
+  int field_mode;             /* 0 off, 1 Gaussian random field */
+  int field_steps;            /* T1 of the interval (steps under the field) */
+  double field_eps;           /* amplitude eps */
+  double field_sigma;         /* correlation length (reference: 32) */
 } clbm_run_desc;
 
 typedef struct clbm_ctx clbm_ctx;
@@ -246,6 +257,14 @@ int clbm_set_step_variant(clbm_ctx *ctx, int variant);
  * write_fluid_vtk prints (src/lbm_src/write_vtk.cpp:8-53). */
 int clbm_macro_fields(clbm_ctx *ctx, int run, int clone, double *rho,
                       double *ux, double *uy);
+
+/* The random body-force field a clone used in the last interval, as FP64 in
+ * the reference's map order y + Dy*x (Dx*Dy values; map may be NULL), and
+ * the number of circulant-embedding eigenvalues below -1e-15 that were set to
+ * zero (*negative, nullable; the reference flags them as an error,
+ * generate_random_field.cpp:145-151). */
+int clbm_get_field_map(clbm_ctx *ctx, int run, int clone, double *map,
+                       int *negative);
 
 /* ---- lineage reconstruction (post_processing/reconstruction.cpp:35-109) ----
  * clbm_enable_history(ctx, max_intervals), before the first interval, keeps
