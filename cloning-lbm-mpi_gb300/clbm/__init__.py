@@ -330,7 +330,7 @@ class Sampler:
     def autotune(self, launches: int = 5, measure: bool = True):
         """Returns (best variant, ms per launch of every variant)."""
         best, nv = C.c_int(), C.c_int()
-        ms = np.zeros(32)
+        ms = np.zeros(64)
         check(lib().clbm_autotune(self.h, launches, C.byref(best), _p(ms) if measure else None,
                                   C.byref(nv)), "clbm_autotune")
         return best.value, ms[:nv.value]

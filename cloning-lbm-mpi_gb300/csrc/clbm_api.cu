@@ -68,6 +68,8 @@ struct clbm_ctx {
   int max_nodes = 0;
   int total_tiles[3] = {0, 0, 0};
   int step_variant = 0;  // FP32 step launch variant (clbm_autotune)
+  int temporal_cs = 0;   // > 0: FP32 intervals run cluster-resident with this cluster size
+  int temporal_variant = 0;
   bool pending = false;  // a clone step's copies/perturbations await the next interval
   // random body-force fields (forcing variant)
   bool any_field = false;
@@ -499,6 +501,7 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
                 c->d.prefactors, c->d.snaps, c->d.state, c->d.err, c->d_maps};
   if ((e = launch_reseed(f64, ra, c->total_blocks, s)) != cudaSuccess) return e;
   int cur = 1 - sbuf;
+  const bool temporal = !f64 && c->temporal_cs > 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (prof) {
     if ((size_t)c->ev_used + 2 > c->ev.size()) {
@@ -514,13 +517,26 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
     c->prof_steps += steps;
     if ((e = cudaEventRecord(e0, s)) != cudaSuccess) return e;
   }
-  for (int t = 0; t < steps; t++) {
-    StepArgs a{c->d.runs, c->nruns, t, c->pop[cur], c->pop[1 - cur], c->d.terms, c->d.term_slab,
-               c->d.err, c->total_clones, c->max_nodes,
-               {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}, c->d_maps};
-    if ((e = launch_step(f64, t == steps - 1, a, c->total_blocks, s, c->step_variant)) != cudaSuccess)
-      return e;
-    cur = 1 - cur;
+  if (temporal) {
+    // the whole interval on chip: P_0 from the reseed output, S_T where the
+    // streaming sequence would leave it
+    const int dst = (steps % 2 == 1) ? sbuf : 1 - sbuf;
+    for (int r = 0; r < c->nruns; r++) {
+      const RunDev &R = c->runs_h[r];
+      TemporalArgs ta{c->d.runs, r, steps, (const float *)c->pop[1 - sbuf], (float *)c->pop[dst],
+                      (float *)c->d.terms, c->d.term_slab, c->d.err, c->d_maps};
+      if ((e = launch_temporal(ta, c->temporal_cs, c->temporal_variant, R.nclones, R.W, R.H, s)) != cudaSuccess)
+        return e;
+    }
+  } else {
+    for (int t = 0; t < steps; t++) {
+      StepArgs a{c->d.runs, c->nruns, t, c->pop[cur], c->pop[1 - cur], c->d.terms, c->d.term_slab,
+                 c->d.err, c->total_clones, c->max_nodes,
+                 {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}, c->d_maps};
+      if ((e = launch_step(f64, t == steps - 1, a, c->total_blocks, s, c->step_variant)) != cudaSuccess)
+        return e;
+      cur = 1 - cur;
+    }
   }
   if (prof && (e = cudaEventRecord(e1, s)) != cudaSuccess) return e;
   if ((e = launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, s)) != cudaSuccess) return e;
@@ -750,6 +766,21 @@ extern "C" int clbm_profile_read(clbm_ctx *c, double *step_ms, int *nsteps) {
   return CLBM_OK;
 }
 
+// Variant numbering: 0 .. step_variant_count()-1 are the streaming step
+// launches; after them, for cluster sizes 1, 2, 4, 8, 16 (index log2), the
+// cluster-resident interval kernel's thread configurations.
+static void apply_variant(clbm_ctx *c, int v) {
+  const int nv = step_variant_count();
+  if (v < nv) {
+    c->step_variant = v;
+    c->temporal_cs = 0;
+  } else {
+    const int q = v - nv;
+    c->temporal_cs = 1 << (q / temporal_variant_count());
+    c->temporal_variant = q % temporal_variant_count();
+  }
+}
+
 // Autotuner: time every FP32 step variant on this context's own workload and
 // keep the fastest.  It runs at an interval boundary, reading the current
 // state and writing the idle buffer (overwritten by the next interval's first
@@ -764,7 +795,7 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
                              int *nvariants) {
   if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
   const int nv = step_variant_count();
-  if (nvariants) *nvariants = nv;
+  if (nvariants) *nvariants = nv + 5 * temporal_variant_count();
   if (c->precision != CLBM_FP32) {
     if (best) *best = 0;
     return CLBM_OK;
@@ -779,7 +810,7 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
-      c->step_variant = it->second;
+      apply_variant(c, it->second);
       if (best) *best = it->second;
       return CLBM_OK;
     }
@@ -814,9 +845,48 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
       arg = v;
     }
   }
+  // cluster-resident candidates, timed per step over a full-length interval
+  // (their HBM load and store are amortised over the steps)
+  const int tsteps = std::min(c->max_steps, 100);
+  int t_cs = 0, t_var = 0;
+  for (int cs = 1; cs <= 16; cs *= 2) {
+    for (int tv = 0; tv < temporal_variant_count(); tv++) {
+      const int vidx = nv + (31 - __builtin_clz((unsigned)cs)) * temporal_variant_count() + tv;
+      if (ms_per_variant) ms_per_variant[vidx] = -1.0;
+      bool ok = true;
+      for (const RunDev &R : c->runs_h)
+        if (R.H % cs || temporal_max_clusters(cs, tv, R.W, R.H) < 1) ok = false;
+      if (!ok) continue;
+      cudaError_t e = cudaEventRecord(e0, c->stream);
+      for (int r = 0; r < c->nruns && e == cudaSuccess; r++) {
+        const RunDev &R = c->runs_h[r];
+        TemporalArgs ta{c->d.runs, r, tsteps, (const float *)c->pop[c->s_buf], (float *)c->pop[1 - c->s_buf],
+                        (float *)c->d.terms, c->d.term_slab, c->d.err, c->d_maps};
+        e = launch_temporal(ta, cs, tv, R.nclones, R.W, R.H, c->stream);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) {  // this shape cannot run here: skip it
+        cudaGetLastError();
+        continue;
+      }
+      const double per = ms / tsteps;
+      if (ms_per_variant) ms_per_variant[vidx] = per;
+      if (per < best_ms) {
+        best_ms = per;
+        t_cs = cs;
+        t_var = tv;
+        arg = vidx;
+      }
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  c->step_variant = arg;
+  c->temporal_cs = t_cs;
+  c->temporal_variant = t_var;
+  if (!t_cs) c->step_variant = arg;
   destroy_graphs(c);
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
@@ -828,8 +898,17 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
 
 extern "C" int clbm_set_step_variant(clbm_ctx *c, int variant) {
   if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
-  if (variant < 0 || variant >= step_variant_count()) return fail(CLBM_ERR_INVALID, "no such variant");
-  c->step_variant = variant;
+  if (variant < 0 || variant >= step_variant_count() + 5 * temporal_variant_count())
+    return fail(CLBM_ERR_INVALID, "no such variant");
+  if (variant >= step_variant_count()) {
+    if (c->precision != CLBM_FP32) return fail(CLBM_ERR_INVALID, "cluster-resident intervals are FP32 only");
+    const int q = variant - step_variant_count();
+    const int cs = 1 << (q / temporal_variant_count()), tv = q % temporal_variant_count();
+    for (const RunDev &R : c->runs_h)
+      if (R.H % cs || temporal_max_clusters(cs, tv, R.W, R.H) < 1)
+        return fail(CLBM_ERR_INVALID, "cluster shape does not fit this workload");
+  }
+  apply_variant(c, variant);
   destroy_graphs(c);
   return CLBM_OK;
 }

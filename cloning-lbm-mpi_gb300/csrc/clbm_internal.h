@@ -77,6 +77,18 @@ struct StepArgs {
   const float *maps;  // random body-force fields (nullable)
 };
 
+struct TemporalArgs {
+  const RunDev *runs;
+  int run;
+  int steps;
+  const float *src;   // P_0 (post-collision) of every clone of the run
+  float *dst;         // S_T (pre-collision) after the interval
+  float *terms;       // base of the drag-term slabs
+  long long term_slab;
+  unsigned *err;
+  const float *maps;  // random body-force fields (nullable)
+};
+
 struct ReseedArgs {
   const RunDev *runs;
   int nruns;
@@ -119,6 +131,10 @@ cudaError_t launch_reconstruct(const double *hist_drag, const int *hist_labels, 
                                int *anc, double *out, cudaStream_t s);
 cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int max_m1, int max_m2,
                           int max_tiles2, cudaStream_t s);
+cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W, int H,
+                            cudaStream_t s);
+int temporal_max_clusters(int cs, int variant, int W, int H);
+int temporal_variant_count();
 cudaError_t launch_scgf(const double *logr, int first, int count, double dT, double *out,
                         cudaStream_t s);
 cudaError_t launch_init_equilibrium(bool f64, const RunDev *runs, int nruns, int run, void *pop,

@@ -49,41 +49,6 @@ __device__ __forceinline__ NodeLoc locate(const RunDev *runs, int nruns) {
 template <bool F64>
 using pop_t = typename std::conditional<F64, double, float>::type;
 
-// Drag terms of one perimeter node, stored at [term][clone] so that the
-// reduction reads them coalesced: West (x = xmin, index y - ymin), East,
-// North (y = ymax, index x - xmin), South.  FP64: the reference's per-node
-// expressions (force.cpp:48, :78, :108, :138).  FP32: shifted variant without
-// the +-1/3 that cancel between West and East.
-template <bool F64>
-__device__ __forceinline__ void store_drag_terms(const RunDev &R, const pop_t<F64> S[9],
-                                                 int x, int y, int clone, pop_t<F64> *T) {
-  const int sy = R.ymax - R.ymin, sx = R.xmax - R.xmin;
-  const int nc = R.nclones;
-  pop_t<F64> west, east, north, south;
-  if constexpr (F64) {
-    double rho, pxx, pxy;
-    pi_ref64(S, rho, pxx, pxy);
-    const double third = 1. / 3.;
-    const double c = R.cforce;
-    west = DADD(DMUL(rho, third), DMUL(c, pxx));
-    east = DSUB(DMUL(-rho, third), DMUL(c, pxx));
-    north = DMUL(-c, pxy);
-    south = DMUL(c, pxy);
-  } else {
-    float drho, pxx, pxy;
-    pi_f32(S, drho, pxx, pxy);
-    const float c = R.f_cforce;
-    west = drho * (1.0f / 3.0f) + c * pxx;
-    east = -west;
-    north = -c * pxy;
-    south = c * pxy;
-  }
-  if (x == R.xmin) T[(long long)(y - R.ymin) * nc + clone] = west;
-  if (x == R.xmax) T[(long long)(sy + 1 + y - R.ymin) * nc + clone] = east;
-  if (y == R.ymax) T[(long long)(2 * (sy + 1) + x - R.xmin) * nc + clone] = north;
-  if (y == R.ymin) T[(long long)(2 * (sy + 1) + sx + 1 + x - R.xmin) * nc + clone] = south;
-}
-
 // map: the node's random-field value when the collision is under the
 // spatial force, beta(x,y) = (1 + eps*map)*beta0 (streamCollCompute.cpp:63)
 template <bool F64>

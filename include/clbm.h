@@ -240,13 +240,17 @@ int clbm_run_sampler(clbm_ctx *ctx, int steps, int intervals, double *rvalues);
 int clbm_profile(clbm_ctx *ctx, int enable);
 int clbm_profile_read(clbm_ctx *ctx, double *step_ms, int *nsteps);
 
-/* Autotuner of the FP32 step kernel: times each launch variant (block size,
- * registers per thread, store caching) on this context's workload, `launches`
- * launches each, at an interval boundary without touching the sampler state,
- * and selects the fastest for the context.  *best = chosen variant,
- * ms_per_variant (nullable, *nvariants entries) = mean milliseconds per
- * launch.  With ms_per_variant NULL a result cached for the same lattices and
- * clone counts is reused.  FP64 contexts have one variant. */
+/* Autotuner of the FP32 interval: times each candidate on this context's
+ * workload at an interval boundary without touching the sampler state, and
+ * selects the fastest.  Candidates: the streaming step kernel's launch
+ * variants (block size, registers per thread, store caching; one launch per
+ * step), then the cluster-resident interval kernel (every clone's populations
+ * in the shared memory of one thread-block cluster for all the steps of an
+ * interval, one launch per interval) for cluster sizes 1, 2, 4, 8, 16 and
+ * three thread counts, where the lattice fits.  *best = chosen candidate,
+ * ms_per_variant (nullable, *nvariants entries, -1 = not runnable here) =
+ * milliseconds per step.  With ms_per_variant NULL a result cached for the same
+ * lattices and clone counts is reused.  FP64 contexts have one variant. */
 int clbm_autotune(clbm_ctx *ctx, int launches, int *best,
                   double *ms_per_variant, int *nvariants);
 int clbm_set_step_variant(clbm_ctx *ctx, int variant);

@@ -1,0 +1,68 @@
+"""The cluster-resident FP32 interval kernel (every clone in the shared
+memory of one thread-block cluster for a whole interval) must give results
+bit-identical to the streaming step kernel: same pull rules, same collision
+arithmetic.  Cases cover cluster sizes 1, 2 and 4 with the square across
+band edges, a width that is not a multiple of 32, copies and perturbations
+between intervals, and the random body-force field."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NSTREAM = 8   # streaming launch variants come first in the autotuner's numbering
+NTHREAD = 3   # thread configurations of the cluster-resident kernel
+
+
+def temporal_variant(cs, tv=0):
+    return NSTREAM + int(np.log2(cs)) * NTHREAD + tv
+
+
+@pytest.mark.parametrize("W,H,side,xc,yc,cs,tv,field", [
+    (64, 24, 6, 16, 12, 1, 0, False),
+    (64, 24, 6, 16, 12, 2, 1, False),
+    (64, 24, 6, 16, 12, 4, 2, False),
+    (200, 32, 8, 50, 16, 4, 0, True),
+    (96, 16, 5, 30, 9, 2, 2, True),
+])
+def test_temporal_equals_streaming(gpu, clbm_lib, orc, W, H, side, xc, yc, cs, tv, field):
+    g = orc.channel_geom(W, H, side, xc, yc)
+    u0, nc, T = 0.05, 5, 21
+    d = clbm_lib.RunDesc(width=g.nx, height=g.ny, xmin=g.xmin, xmax=g.xmax, ymin=g.ymin, ymax=g.ymax,
+                         nclones=nc, ranks=1, tau=0.57, beta=side * u0 * u0 / ((W - 1) * (H - 1)), alpha=8.0,
+                         force_scale=2 / (u0 * u0 * side), dt=u0 / side, perturb_mode=clbm_lib.PERTURB_UNIFORM,
+                         eps=1e-4, seed=7)
+    if field:
+        d.field_mode, d.field_steps, d.field_eps, d.field_sigma = 1, 7, 0.2, 6.0
+    out = []
+    for variant in (4, temporal_variant(cs, tv)):
+        with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T) as s:
+            s.set_step_variant(variant)
+            s.init_equilibrium(0, u0, 1e-3, 7)
+            res = []
+            for t in range(3):
+                s.run_interval(T)
+                res.append(s.drag(0))
+                s.clone_step()
+                res.append(s.clone_result(0)["labels"].astype(np.float64))
+            s.run_interval(T)
+            res.append(s.drag(0))
+            res.extend(s.dump(0, j) for j in range(nc))
+            assert s.error_word() == 0
+            out.append(res)
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
+
+
+def test_autotune_considers_cluster_resident_kernel(gpu, clbm_lib, orc):
+    g = orc.channel_geom(256, 64, 12, 64, 32)
+    d = clbm_lib.RunDesc(width=g.nx, height=g.ny, xmin=g.xmin, xmax=g.xmax, ymin=g.ymin, ymax=g.ymax,
+                         nclones=64, ranks=1, tau=0.55, beta=1e-6, alpha=0.3, force_scale=100.0, dt=0.003)
+    with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=20) as s:
+        s.init_equilibrium(0, 0.04, 1e-3, 3)
+        before = s.dump(0, 5)
+        best, ms = s.autotune(launches=2)
+        assert len(ms) == NSTREAM + 5 * NTHREAD
+        assert (ms[NSTREAM:] > 0).any(), ms
+        assert np.array_equal(s.dump(0, 5), before)
+        s.run_interval(20)
+        assert s.error_word() == 0
