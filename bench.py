@@ -294,6 +294,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--graph", action="store_true", help="replay each interval as a CUDA graph")
+    ap.add_argument("--variant", type=int, default=None,
+                    help="use this interval kernel variant instead of autotuning (profiling)")
     ap.add_argument("--study", choices=["precision", "adjoint"], default=None)
     args = ap.parse_args()
     from clbm import configs
@@ -319,7 +321,11 @@ def main():
     stream = torch.cuda.ExternalStream(s.stream())
     s.run_sampler(wl.steps, max(1, args.warmup - 1))
     # autotune the step kernel's launch variant on this workload (state untouched)
-    best, tune_ms = s.autotune(launches=5)
+    if args.variant is None:
+        best, tune_ms = s.autotune(launches=5)
+    else:
+        s.set_step_variant(args.variant)
+        best, tune_ms = args.variant, []
     s.run_sampler(wl.steps, 1)
     s.sync()
 
