@@ -52,37 +52,60 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
     for (int k = 0; k < 9; k++) A[opp_of(k) * nb + i] = src[k * plane + n];
   }
   cluster.sync();
+  const int npt = (nb + THREADS - 1) / THREADS;  // uniform trip count for the warp votes
   for (int t = 0; t < a.steps; t++) {
     const bool gather = (t & 1) == 0, last = t == a.steps - 1;
     float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
-    for (int i = threadIdx.x; i < nb; i += THREADS) {
-      const int ly = i / W, x = i - ly * W, y = row0 + ly;
-      const long long n = (long long)y * W + x;
+    for (int j = 0; j < npt; j++) {
+      const int i = threadIdx.x + j * THREADS;
+      const bool valid = i < nb;
+      const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = row0 + ly;
       const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
-      const int mask = (in_box || y == 0 || y == H - 1) ? bounce_mask(R, x, y) : 0;
-      if (mask & 512) {  // inside the square
-        if (last) {
-#pragma unroll
-          for (int k = 0; k < 9; k++) dst[k * plane + n] = 0.0f;
-        }
-        continue;
-      }
+      const bool near = in_box || y == 0 || y == H - 1;
+      const bool edge = cs > 1 && (ly == 0 || ly == rows - 1);
+      // bulk warps: every source and target in this CTA's shared memory, no
+      // bounce-back; decided per warp so the two paths do not diverge
+      const bool bulk = __all_sync(0xffffffffu, !valid || (!near && !edge));
+      if (!valid) continue;
+      const long long n = (long long)y * W + x;
       const int xl = (x == 0) ? W - 1 : x - 1, xr = (x == W - 1) ? 0 : x + 1;
       float S[9];
+      int mask = 0;
+      if (bulk) {
 #pragma unroll
-      for (int k = 0; k < 9; k++) {
-        if (!gather || ((mask >> k) & 1)) {
-          S[k] = A[k * nb + i];
-        } else {
-          const int cx = cx_of(k), cy = cy_of(k);
-          const int sx = cx == 1 ? xl : (cx == -1 ? xr : x);
-          const int sl = ly - cy;  // source row, band-local
-          const float *base = sl < 0 ? prev : (sl >= rows ? next : A);
-          const int sr = sl < 0 ? rows - 1 : (sl >= rows ? 0 : sl);
-          S[k] = base[opp_of(k) * nb + sr * W + sx];
+        for (int k = 0; k < 9; k++) {
+          if (!gather) {
+            S[k] = A[k * nb + i];
+          } else {
+            const int cx = cx_of(k), cy = cy_of(k);
+            const int sx = cx == 1 ? xl : (cx == -1 ? xr : x);
+            S[k] = A[opp_of(k) * nb + (ly - cy) * W + sx];
+          }
         }
+      } else {
+        mask = near ? bounce_mask(R, x, y) : 0;
+        if (mask & 512) {  // inside the square
+          if (last) {
+#pragma unroll
+            for (int k = 0; k < 9; k++) dst[k * plane + n] = 0.0f;
+          }
+          continue;
+        }
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+          if (!gather || ((mask >> k) & 1)) {
+            S[k] = A[k * nb + i];
+          } else {
+            const int cx = cx_of(k), cy = cy_of(k);
+            const int sx = cx == 1 ? xl : (cx == -1 ? xr : x);
+            const int sl = ly - cy;  // source row, band-local
+            const float *base = sl < 0 ? prev : (sl >= rows ? next : A);
+            const int sr = sl < 0 ? rows - 1 : (sl >= rows ? 0 : sl);
+            S[k] = base[opp_of(k) * nb + sr * W + sx];
+          }
+        }
+        if (in_box) store_drag_terms<false>(R, S, x, y, clone, terms);
       }
-      if (in_box) store_drag_terms<false>(R, S, x, y, clone, terms);
       if (last) {
         float d = 0.f;
 #pragma unroll
@@ -99,21 +122,34 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
       float P[9];
       const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
       if (!(drho > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
+      if (bulk) {
 #pragma unroll
-      for (int k = 0; k < 9; k++) {
-        const int ok = opp_of(k);
-        if (!gather || ((mask >> ok) & 1)) {
-          A[ok * nb + i] = P[k];
-        } else {
-          const int cx = cx_of(k), cy = cy_of(k);
-          const int tx = cx == 1 ? xr : (cx == -1 ? xl : x);
-          const int ty = y + cy;
-          if (ty < 0 || ty >= H) continue;
-          if (tx > R.xmin && tx < R.xmax && ty > R.ymin && ty < R.ymax) continue;  // into the square
-          const int tl = ly + cy;
-          float *base = tl < 0 ? prev : (tl >= rows ? next : A);
-          const int tr = tl < 0 ? rows - 1 : (tl >= rows ? 0 : tl);
-          base[k * nb + tr * W + tx] = P[k];
+        for (int k = 0; k < 9; k++) {
+          if (!gather) {
+            A[opp_of(k) * nb + i] = P[k];
+          } else {
+            const int cx = cx_of(k), cy = cy_of(k);
+            const int tx = cx == 1 ? xr : (cx == -1 ? xl : x);
+            A[k * nb + (ly + cy) * W + tx] = P[k];
+          }
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+          const int ok = opp_of(k);
+          if (!gather || ((mask >> ok) & 1)) {
+            A[ok * nb + i] = P[k];
+          } else {
+            const int cx = cx_of(k), cy = cy_of(k);
+            const int tx = cx == 1 ? xr : (cx == -1 ? xl : x);
+            const int ty = y + cy;
+            if (ty < 0 || ty >= H) continue;
+            if (tx > R.xmin && tx < R.xmax && ty > R.ymin && ty < R.ymax) continue;  // into the square
+            const int tl = ly + cy;
+            float *base = tl < 0 ? prev : (tl >= rows ? next : A);
+            const int tr = tl < 0 ? rows - 1 : (tl >= rows ? 0 : tl);
+            base[k * nb + tr * W + tx] = P[k];
+          }
         }
       }
     }
