@@ -523,7 +523,7 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
     const int dst = (steps % 2 == 1) ? sbuf : 1 - sbuf;
     for (int r = 0; r < c->nruns; r++) {
       const RunDev &R = c->runs_h[r];
-      TemporalArgs ta{c->d.runs, r, steps, (const float *)c->pop[1 - sbuf], (float *)c->pop[dst],
+      TemporalArgs ta{c->runs_h[r], r, steps, (const float *)c->pop[1 - sbuf], (float *)c->pop[dst],
                       (float *)c->d.terms, c->d.term_slab, c->d.err, c->d_maps};
       if ((e = launch_temporal(ta, c->temporal_cs, c->temporal_variant, R.nclones, R.W, R.H, s)) != cudaSuccess)
         return e;
@@ -860,7 +860,7 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
       cudaError_t e = cudaEventRecord(e0, c->stream);
       for (int r = 0; r < c->nruns && e == cudaSuccess; r++) {
         const RunDev &R = c->runs_h[r];
-        TemporalArgs ta{c->d.runs, r, tsteps, (const float *)c->pop[c->s_buf], (float *)c->pop[1 - c->s_buf],
+        TemporalArgs ta{c->runs_h[r], r, tsteps, (const float *)c->pop[c->s_buf], (float *)c->pop[1 - c->s_buf],
                         (float *)c->d.terms, c->d.term_slab, c->d.err, c->d_maps};
         e = launch_temporal(ta, cs, tv, R.nclones, R.W, R.H, c->stream);
       }

@@ -78,7 +78,7 @@ struct StepArgs {
 };
 
 struct TemporalArgs {
-  const RunDev *runs;
+  RunDev rd;          // the run, by value: kernel-parameter space, never aliased
   int run;
   int steps;
   const float *src;   // P_0 (post-collision) of every clone of the run

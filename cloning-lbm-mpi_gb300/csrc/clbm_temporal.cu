@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
   cg::cluster_group cluster = cg::this_cluster();
   const int cs = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
-  const RunDev &R = a.runs[a.run];
+  const RunDev &R = a.rd;
   const int clone = blockIdx.x / cs;
   const int W = R.W, H = R.H;
   const int rows = H / cs, row0 = rank * rows;
