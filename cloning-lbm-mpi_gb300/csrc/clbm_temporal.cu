@@ -30,7 +30,10 @@ namespace clbm {
 
 template <int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) {
-  extern __shared__ float A[];  // [9][R*W]
+  // A[node * 9 + k]: a node's nine values together (stride 9 words: no bank
+  // conflicts across a warp), so every access is a base register plus an
+  // immediate offset
+  extern __shared__ float A[];
   cg::cluster_group cluster = cg::this_cluster();
   const int cs = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
@@ -49,43 +52,58 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
   for (int i = threadIdx.x; i < nb; i += THREADS) {
     const long long n = (long long)row0 * W + i;
 #pragma unroll
-    for (int k = 0; k < 9; k++) A[opp_of(k) * nb + i] = src[k * plane + n];
+    for (int k = 0; k < 9; k++) A[i * 9 + opp_of(k)] = src[k * plane + n];
   }
+  // bulk[j]: the whole warp's node j is away from band edges, walls and the
+  // square, so all its neighbours are in this CTA and nothing bounces back
+  const int npt = (nb + THREADS - 1) / THREADS;
+  unsigned bulk_bits = 0;
+  for (int j = 0; j < npt && j < 32; j++) {
+    const int i = threadIdx.x + j * THREADS;
+    const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = row0 + ly;
+    const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+    const bool ok = i >= nb || !(in_box || y == 0 || y == H - 1 || (cs > 1 && (ly == 0 || ly == rows - 1)));
+    if (__all_sync(0xffffffffu, ok)) bulk_bits |= 1u << j;
+  }
+  const int rowstep = W * 9;  // one row in A, in words
   cluster.sync();
-  const int npt = (nb + THREADS - 1) / THREADS;  // uniform trip count for the warp votes
   for (int t = 0; t < a.steps; t++) {
     const bool gather = (t & 1) == 0, last = t == a.steps - 1;
     float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
     for (int j = 0; j < npt; j++) {
       const int i = threadIdx.x + j * THREADS;
-      const bool valid = i < nb;
+      if (i >= nb) continue;
       const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = row0 + ly;
-      const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
-      const bool near = in_box || y == 0 || y == H - 1;
-      const bool edge = cs > 1 && (ly == 0 || ly == rows - 1);
-      // bulk warps: every source and target in this CTA's shared memory, no
-      // bounce-back; decided per warp so the two paths do not diverge
-      const bool bulk = __all_sync(0xffffffffu, !valid || (!near && !edge));
-      if (!valid) continue;
-      const long long n = (long long)y * W + x;
-      const int xl = (x == 0) ? W - 1 : x - 1, xr = (x == W - 1) ? 0 : x + 1;
+      const bool bulk = j < 32 && ((bulk_bits >> j) & 1u);
+      // source / target columns: x-1 and x+1 with the periodic wrap
+      const int cm = (x == 0 ? i + W - 1 : i - 1) * 9;
+      const int c0 = i * 9;
+      const int cp = (x == W - 1 ? i - (W - 1) : i + 1) * 9;
       float S[9];
       int mask = 0;
+      bool in_box = false;
       if (bulk) {
+        if (gather) {
+          // S(n,k) = A[n - c_k][opp k]
+          S[0] = A[c0 + 0];
+          S[1] = A[cm + 3];
+          S[2] = A[c0 - rowstep + 4];
+          S[3] = A[cp + 1];
+          S[4] = A[c0 + rowstep + 2];
+          S[5] = A[cm - rowstep + 7];
+          S[6] = A[cp - rowstep + 8];
+          S[7] = A[cp + rowstep + 5];
+          S[8] = A[cm + rowstep + 6];
+        } else {
 #pragma unroll
-        for (int k = 0; k < 9; k++) {
-          if (!gather) {
-            S[k] = A[k * nb + i];
-          } else {
-            const int cx = cx_of(k), cy = cy_of(k);
-            const int sx = cx == 1 ? xl : (cx == -1 ? xr : x);
-            S[k] = A[opp_of(k) * nb + (ly - cy) * W + sx];
-          }
+          for (int k = 0; k < 9; k++) S[k] = A[c0 + k];
         }
       } else {
-        mask = near ? bounce_mask(R, x, y) : 0;
+        in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+        mask = (in_box || y == 0 || y == H - 1) ? bounce_mask(R, x, y) : 0;
         if (mask & 512) {  // inside the square
           if (last) {
+            const long long n = (long long)y * W + x;
 #pragma unroll
             for (int k = 0; k < 9; k++) dst[k * plane + n] = 0.0f;
           }
@@ -94,19 +112,20 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
 #pragma unroll
         for (int k = 0; k < 9; k++) {
           if (!gather || ((mask >> k) & 1)) {
-            S[k] = A[k * nb + i];
+            S[k] = A[c0 + k];
           } else {
             const int cx = cx_of(k), cy = cy_of(k);
-            const int sx = cx == 1 ? xl : (cx == -1 ? xr : x);
-            const int sl = ly - cy;  // source row, band-local
+            const int sxc = cx == 1 ? cm : (cx == -1 ? cp : c0);  // column, row ly
+            const int sl = ly - cy;                                 // source row, band-local
             const float *base = sl < 0 ? prev : (sl >= rows ? next : A);
-            const int sr = sl < 0 ? rows - 1 : (sl >= rows ? 0 : sl);
-            S[k] = base[opp_of(k) * nb + sr * W + sx];
+            const int roff = sl < 0 ? (rows - 1 - ly) * rowstep : (sl >= rows ? -ly * rowstep : -cy * rowstep);
+            S[k] = base[sxc + roff + opp_of(k)];
           }
         }
         if (in_box) store_drag_terms<false>(R, S, x, y, clone, terms);
       }
       if (last) {
+        const long long n = (long long)y * W + x;
         float d = 0.f;
 #pragma unroll
         for (int k = 0; k < 9; k++) {
@@ -118,37 +137,43 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
       }
       float beta = R.f_beta;
       if (R.field_mode && t + 1 < R.field_steps && a.maps)
-        beta *= 1.0f + R.f_field_eps * a.maps[R.map_base + (long long)clone * R.nodes + n];
+        beta *= 1.0f + R.f_field_eps * a.maps[R.map_base + (long long)clone * R.nodes + (long long)y * W + x];
       float P[9];
       const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
       if (!(drho > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
       if (bulk) {
+        if (gather) {
+          // P(n,k) -> A[n + c_k][k]
+          A[c0 + 0] = P[0];
+          A[cp + 1] = P[1];
+          A[c0 + rowstep + 2] = P[2];
+          A[cm + 3] = P[3];
+          A[c0 - rowstep + 4] = P[4];
+          A[cp + rowstep + 5] = P[5];
+          A[cm + rowstep + 6] = P[6];
+          A[cm - rowstep + 7] = P[7];
+          A[cp - rowstep + 8] = P[8];
+        } else {
 #pragma unroll
-        for (int k = 0; k < 9; k++) {
-          if (!gather) {
-            A[opp_of(k) * nb + i] = P[k];
-          } else {
-            const int cx = cx_of(k), cy = cy_of(k);
-            const int tx = cx == 1 ? xr : (cx == -1 ? xl : x);
-            A[k * nb + (ly + cy) * W + tx] = P[k];
-          }
+          for (int k = 0; k < 9; k++) A[c0 + opp_of(k)] = P[k];
         }
       } else {
 #pragma unroll
         for (int k = 0; k < 9; k++) {
           const int ok = opp_of(k);
           if (!gather || ((mask >> ok) & 1)) {
-            A[ok * nb + i] = P[k];
+            A[c0 + ok] = P[k];
           } else {
             const int cx = cx_of(k), cy = cy_of(k);
-            const int tx = cx == 1 ? xr : (cx == -1 ? xl : x);
+            const int tx = cx == 1 ? (x == W - 1 ? 0 : x + 1) : (cx == -1 ? (x == 0 ? W - 1 : x - 1) : x);
             const int ty = y + cy;
             if (ty < 0 || ty >= H) continue;
             if (tx > R.xmin && tx < R.xmax && ty > R.ymin && ty < R.ymax) continue;  // into the square
+            const int txc = cx == 1 ? cp : (cx == -1 ? cm : c0);
             const int tl = ly + cy;
             float *base = tl < 0 ? prev : (tl >= rows ? next : A);
-            const int tr = tl < 0 ? rows - 1 : (tl >= rows ? 0 : tl);
-            base[k * nb + tr * W + tx] = P[k];
+            const int roff = tl < 0 ? (rows - 1 - ly) * rowstep : (tl >= rows ? -ly * rowstep : cy * rowstep);
+            base[txc + roff + k] = P[k];
           }
         }
       }
