@@ -54,41 +54,34 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
 #pragma unroll
     for (int k = 0; k < 9; k++) A[i * 9 + opp_of(k)] = src[k * plane + n];
   }
-  // Within a step the band's interior rows (1 .. rows-2) read and write only
-  // this CTA's shared memory, and the slots they touch are never touched by
-  // the neighbouring bands in the adjacent step; only the edge rows (0 and
-  // rows-1) exchange with the neighbours.  So each step processes the interior
-  // after a CTA barrier, then waits for the cluster barrier of the previous
-  // step (split arrive / wait), then processes the edge rows: the cluster
-  // barrier's latency hides behind the interior work.
-  const int nint = rows > 2 ? (rows - 2) * W : 0;
-  const int nedge = nb - nint;  // rows 0 and rows-1
-  const int npt_int = (nint + THREADS - 1) / THREADS;
-  const int npt_edge = (nedge + THREADS - 1) / THREADS;
-  // bulk[j]: the whole warp's interior node j is away from walls and the
+  // bulk[j]: the whole warp's node j is away from band edges, walls and the
   // square, so all its neighbours are in this CTA and nothing bounces back
+  const int npt = (nb + THREADS - 1) / THREADS;
   unsigned bulk_bits = 0;
-  for (int j = 0; j < npt_int && j < 32; j++) {
-    const int i = W + threadIdx.x + j * THREADS;
+  for (int j = 0; j < npt && j < 32; j++) {
+    const int i = threadIdx.x + j * THREADS;
     const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = row0 + ly;
     const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
-    const bool ok = i >= W + nint || !(in_box || y == 0 || y == H - 1);
+    const bool ok = i >= nb || !(in_box || y == 0 || y == H - 1 || (cs > 1 && (ly == 0 || ly == rows - 1)));
     if (__all_sync(0xffffffffu, ok)) bulk_bits |= 1u << j;
   }
   const int rowstep = W * 9;  // one row in A, in words
-  __syncthreads();
-  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+  cluster.sync();
   for (int t = 0; t < a.steps; t++) {
     const bool gather = (t & 1) == 0, last = t == a.steps - 1;
     float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
-    auto update = [&](const int i, const bool bulk) {
+    for (int j = 0; j < npt; j++) {
+      const int i = threadIdx.x + j * THREADS;
+      if (i >= nb) continue;
       const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = row0 + ly;
+      const bool bulk = j < 32 && ((bulk_bits >> j) & 1u);
       // source / target columns: x-1 and x+1 with the periodic wrap
       const int cm = (x == 0 ? i + W - 1 : i - 1) * 9;
       const int c0 = i * 9;
       const int cp = (x == W - 1 ? i - (W - 1) : i + 1) * 9;
       float S[9];
       int mask = 0;
+      bool in_box = false;
       if (bulk) {
         if (gather) {
           // S(n,k) = A[n - c_k][opp k]
@@ -106,7 +99,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
           for (int k = 0; k < 9; k++) S[k] = A[c0 + k];
         }
       } else {
-        const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+        in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
         mask = (in_box || y == 0 || y == H - 1) ? bounce_mask(R, x, y) : 0;
         if (mask & 512) {  // inside the square
           if (last) {
@@ -114,7 +107,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
 #pragma unroll
             for (int k = 0; k < 9; k++) dst[k * plane + n] = 0.0f;
           }
-          return;
+          continue;
         }
 #pragma unroll
         for (int k = 0; k < 9; k++) {
@@ -140,7 +133,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
           d += S[k];
         }
         if (!(d > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
-        return;
+        continue;
       }
       float beta = R.f_beta;
       if (R.field_mode && t + 1 < R.field_steps && a.maps)
@@ -184,21 +177,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
           }
         }
       }
-    };
-    __syncthreads();  // this CTA's writes of the previous step
-    for (int j = 0; j < npt_int; j++) {
-      const int i = W + threadIdx.x + j * THREADS;
-      if (i < W + nint) update(i, j < 32 && ((bulk_bits >> j) & 1u));
     }
-    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");  // neighbours' previous step
-    for (int j = 0; j < npt_edge; j++) {
-      const int e = threadIdx.x + j * THREADS;
-      if (e < nedge) update(e < W ? e : (rows - 1) * W + (e - W), false);
-    }
-    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    cluster.sync();
   }
-  // stay resident until no neighbour can still read this CTA's shared memory
-  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
 struct TemporalVariant {
