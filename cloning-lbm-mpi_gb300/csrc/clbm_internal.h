@@ -133,7 +133,7 @@ cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int m
                           int max_tiles2, cudaStream_t s);
 cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W, int H,
                             cudaStream_t s);
-int temporal_max_clusters(int cs, int variant, int W, int H);
+int temporal_max_clusters(int cs, int variant, int W, int H, bool field);
 int temporal_variant_count();
 cudaError_t launch_scgf(const double *logr, int first, int count, double dT, double *out,
                         cudaStream_t s);

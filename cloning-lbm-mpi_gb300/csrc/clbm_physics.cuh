@@ -142,60 +142,78 @@ __device__ __forceinline__ void collide_f32(const float g[9], float out[9], floa
   }
 }
 
+// FP32 body force of a node under a random field: beta (1 + eps m), with
+// explicit rounding steps so that no kernel contracts or reorders it
+// differently (the streaming and cluster-resident kernels must agree bit for
+// bit); eps = 0 gives beta exactly.
+__device__ __forceinline__ float field_beta_f32(float beta, float eps, float m) {
+  return __fmul_rn(beta, __fmaf_rn(eps, m, 1.0f));
+}
+
 // The same collision organised by opposite pairs (k, opp k): they share
 // |c.u|, so with e = c_k.u the equilibria split into an even part
 // w (drho + rho (4.5 e^2 - 1.5 u^2)) and an odd part +-3 w rho e, and the
 // Guo terms into w fb (9 cx e - 3 ux) and +-3 w fb cx.  Returns drho.
+// Every operation is an explicitly rounded intrinsic (the fused multiply-adds
+// chosen here, none left to the compiler), so the result is the same bit for
+// bit in every kernel that inlines it, whatever it knows about beta.
+namespace f32op {
+__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+}  // namespace f32op
+
 __device__ __forceinline__ float collide_f32_pairs(const float g[9], float out[9], float beta,
                                                    float omega, float cforce) {
-  const float drho = ((g[0] + (g[1] + g[3])) + (g[2] + g[4])) + ((g[5] + g[7]) + (g[6] + g[8]));
-  const float jx = (g[1] - g[3]) + ((g[5] - g[7]) + (g[8] - g[6]));
-  const float jy = (g[2] - g[4]) + ((g[5] - g[7]) + (g[6] - g[8]));
-  const float rho = 1.0f + drho;
+  using namespace f32op;
+  const float a57 = add(g[5], g[7]), a68 = add(g[6], g[8]);
+  const float s57 = sub(g[5], g[7]);
+  const float drho = add(add(add(g[0], add(g[1], g[3])), add(g[2], g[4])), add(a57, a68));
+  const float jx = add(sub(g[1], g[3]), add(s57, sub(g[8], g[6])));
+  const float jy = add(sub(g[2], g[4]), add(s57, sub(g[6], g[8])));
+  const float rho = add(1.0f, drho);
   const float inv = __frcp_rn(rho);
-  const float ux = (jx + 0.5f * beta) * inv;
-  const float uy = jy * inv;
-  const float u2 = 1.5f * (ux * ux + uy * uy);
-  const float fb = cforce * beta;
-  const float om1 = 1.0f - omega;
-  const float base = drho - rho * u2;      // even part before the e^2 term (per unit weight)
-  const float fx = -3.0f * fb * ux;        // Guo even part for cx = 0 (per unit weight)
+  const float ux = mul(fma(0.5f, beta, jx), inv);
+  const float uy = mul(jy, inv);
+  const float u2 = mul(1.5f, fma(ux, ux, mul(uy, uy)));
+  const float fb = mul(cforce, beta);
+  const float fb3 = mul(3.0f, fb), fb9 = mul(9.0f, fb);
+  const float om1 = sub(1.0f, omega);
+  const float base = fma(-rho, u2, drho);  // even part before the e^2 term (per unit weight)
+  const float fx = mul(mul(-3.0f, fb), ux);  // Guo even part for cx = 0 (per unit weight)
   // k = 0
-  out[0] = om1 * g[0] + (4.0f / 9.0f) * (omega * base + fx);
-  const float r45 = 4.5f * rho, r3 = 3.0f * rho;
+  out[0] = fma(om1, g[0], mul(4.0f / 9.0f, fma(omega, base, fx)));
+  const float r45 = mul(4.5f, rho), or3 = mul(omega, mul(3.0f, rho));
   // axis pairs (1,3): e = ux, cx = 1; (2,4): e = uy, cx = 0
   {
-    const float w = 1.0f / 9.0f;
-    const float e = ux;
-    const float ev = w * (omega * (base + r45 * e * e) + (9.0f * fb * e + fx));
-    const float od = w * (omega * r3 * e + 3.0f * fb);
-    out[1] = om1 * g[1] + (ev + od);
-    out[3] = om1 * g[3] + (ev - od);
+    const float w = 1.0f / 9.0f, e = ux;
+    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(fb9, e, fx)));
+    const float od = mul(w, fma(or3, e, fb3));
+    out[1] = fma(om1, g[1], add(ev, od));
+    out[3] = fma(om1, g[3], sub(ev, od));
   }
   {
-    const float w = 1.0f / 9.0f;
-    const float e = uy;
-    const float ev = w * (omega * (base + r45 * e * e) + fx);
-    const float od = w * (omega * r3 * e);
-    out[2] = om1 * g[2] + (ev + od);
-    out[4] = om1 * g[4] + (ev - od);
+    const float w = 1.0f / 9.0f, e = uy;
+    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fx));
+    const float od = mul(w, mul(or3, e));
+    out[2] = fma(om1, g[2], add(ev, od));
+    out[4] = fma(om1, g[4], sub(ev, od));
   }
   // diagonal pairs (5,7): e = ux + uy, cx = 1; (6,8): e = uy - ux, cx = -1
   {
-    const float w = 1.0f / 36.0f;
-    const float e = ux + uy;
-    const float ev = w * (omega * (base + r45 * e * e) + (9.0f * fb * e + fx));
-    const float od = w * (omega * r3 * e + 3.0f * fb);
-    out[5] = om1 * g[5] + (ev + od);
-    out[7] = om1 * g[7] + (ev - od);
+    const float w = 1.0f / 36.0f, e = add(ux, uy);
+    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(fb9, e, fx)));
+    const float od = mul(w, fma(or3, e, fb3));
+    out[5] = fma(om1, g[5], add(ev, od));
+    out[7] = fma(om1, g[7], sub(ev, od));
   }
   {
-    const float w = 1.0f / 36.0f;
-    const float e = uy - ux;
-    const float ev = w * (omega * (base + r45 * e * e) + (-9.0f * fb * e + fx));
-    const float od = w * (omega * r3 * e - 3.0f * fb);
-    out[6] = om1 * g[6] + (ev + od);
-    out[8] = om1 * g[8] + (ev - od);
+    const float w = 1.0f / 36.0f, e = sub(uy, ux);
+    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(-fb9, e, fx)));
+    const float od = mul(w, fma(or3, e, -fb3));
+    out[6] = fma(om1, g[6], add(ev, od));
+    out[8] = fma(om1, g[8], sub(ev, od));
   }
   return drho;
 }
@@ -203,16 +221,21 @@ __device__ __forceinline__ float collide_f32_pairs(const float g[9], float out[9
 // Drag terms from shifted populations, rest parts removed analytically:
 //   pi_xx = sum_{cx!=0} g - drho/3 - rho ux^2,  pi_xy = g5 - g6 + g7 - g8 - rho ux uy
 // and the West/East rho/3 becomes drho/3 (the +-1/3 cancel between sides).
+// (explicitly rounded like collide_f32_pairs)
 __device__ __forceinline__ void pi_f32(const float g[9], float &drho_o, float &pxx, float &pxy) {
-  const float drho = ((g[0] + (g[1] + g[3])) + (g[2] + g[4])) + ((g[5] + g[7]) + (g[6] + g[8]));
-  const float jx = (g[1] - g[3]) + ((g[5] - g[7]) + (g[8] - g[6]));
-  const float jy = (g[2] - g[4]) + ((g[5] - g[7]) + (g[6] - g[8]));
-  const float rho = 1.0f + drho;
-  const float ux = jx / rho, uy = jy / rho;
-  const float sxx = (g[1] + g[3]) + ((g[5] + g[7]) + (g[6] + g[8]));
+  using namespace f32op;
+  const float a57 = add(g[5], g[7]), a68 = add(g[6], g[8]);
+  const float s57 = sub(g[5], g[7]);
+  const float drho = add(add(add(g[0], add(g[1], g[3])), add(g[2], g[4])), add(a57, a68));
+  const float jx = add(sub(g[1], g[3]), add(s57, sub(g[8], g[6])));
+  const float jy = add(sub(g[2], g[4]), add(s57, sub(g[6], g[8])));
+  const float rho = add(1.0f, drho);
+  const float ux = __fdiv_rn(jx, rho), uy = __fdiv_rn(jy, rho);
+  const float sxx = add(add(g[1], g[3]), add(a57, a68));
+  const float rux = mul(rho, ux);
   drho_o = drho;
-  pxx = sxx - drho * (1.0f / 3.0f) - rho * ux * ux;
-  pxy = ((g[5] + g[7]) - (g[6] + g[8])) - rho * ux * uy;
+  pxx = fma(-rux, ux, fma(-drho, 1.0f / 3.0f, sxx));
+  pxy = fma(-rux, uy, sub(a57, a68));
 }
 
 // Drag terms of one perimeter node, stored at [term][clone] so that the
@@ -240,10 +263,10 @@ __device__ __forceinline__ void store_drag_terms(
     float drho, pxx, pxy;
     pi_f32(S, drho, pxx, pxy);
     const float c = R.f_cforce;
-    west = drho * (1.0f / 3.0f) + c * pxx;
+    west = __fmaf_rn(drho, 1.0f / 3.0f, __fmul_rn(c, pxx));
     east = -west;
-    north = -c * pxy;
-    south = c * pxy;
+    north = __fmul_rn(-c, pxy);
+    south = __fmul_rn(c, pxy);
   }
   if (x == R.xmin) T[(long long)(y - R.ymin) * nc + clone] = west;
   if (x == R.xmax) T[(long long)(sy + 1 + y - R.ymin) * nc + clone] = east;

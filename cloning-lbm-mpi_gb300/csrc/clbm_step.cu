@@ -65,7 +65,7 @@ __device__ __forceinline__ void collide_node(const RunDev &R, const pop_t<F64> S
       collide_ref64(S, P, R.beta, R.wcb, R.omega, R.om1);
     }
   } else {
-    const float beta = map ? R.f_beta * (1.0f + R.f_field_eps * *map) : R.f_beta;
+    const float beta = map ? field_beta_f32(R.f_beta, R.f_field_eps, *map) : R.f_beta;
     collide_f32(S, P, beta, R.f_omega, R.f_cforce);
   }
 }
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_step_f32(StepArgs a) {
   } else {
     float beta = R.f_beta;
     if (R.field_mode && a.step + 1 < R.field_steps && a.maps)
-      beta *= 1.0f + R.f_field_eps * a.maps[R.map_base + (long long)clone * R.nodes + n];
+      beta = field_beta_f32(beta, R.f_field_eps, a.maps[R.map_base + (long long)clone * R.nodes + n]);
     drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
   }
   if (!(drho > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);

@@ -28,222 +28,381 @@ namespace cg = cooperative_groups;
 
 namespace clbm {
 
-template <int THREADS, int MINB>
+// Geometry of one CTA's band, shared by both kernels.
+struct Band {
+  int cs, rank, clone, W, H, rows, row0, nb, rowstep;
+  float *prev, *next;
+  long long plane;
+  const float *src;
+  float *dst;
+};
+
+// One node of one step, any position: bounce-back, band edges (distributed
+// shared memory), the square, walls.  i = band-local node index.
+__device__ __forceinline__ void update_general(const TemporalArgs &a, const Band &b, float *A, int i,
+                                               int t, bool gather, bool last, float *terms) {
+  const RunDev &R = a.rd;
+  const int W = b.W, H = b.H, rows = b.rows, rowstep = b.rowstep;
+  const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = b.row0 + ly;
+  const int cm = (x == 0 ? i + W - 1 : i - 1) * 9;
+  const int c0 = i * 9;
+  const int cp = (x == W - 1 ? i - (W - 1) : i + 1) * 9;
+  const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+  const int mask = (in_box || y == 0 || y == H - 1) ? bounce_mask(R, x, y) : 0;
+  const long long n = (long long)y * W + x;
+  if (mask & 512) {  // inside the square
+    if (last) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) b.dst[k * b.plane + n] = 0.0f;
+    }
+    return;
+  }
+  float S[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    if (!gather || ((mask >> k) & 1)) {
+      S[k] = A[c0 + k];
+    } else {
+      const int cx = cx_of(k), cy = cy_of(k);
+      const int sxc = cx == 1 ? cm : (cx == -1 ? cp : c0);  // column, row ly
+      const int sl = ly - cy;                                 // source row, band-local
+      const float *base = sl < 0 ? b.prev : (sl >= rows ? b.next : A);
+      const int roff = sl < 0 ? (rows - 1 - ly) * rowstep : (sl >= rows ? -ly * rowstep : -cy * rowstep);
+      S[k] = base[sxc + roff + opp_of(k)];
+    }
+  }
+  if (in_box) store_drag_terms<false>(R, S, x, y, b.clone, terms);
+  if (last) {
+    float d = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      b.dst[k * b.plane + n] = S[k];
+      d += S[k];
+    }
+    if (!(d > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
+    return;
+  }
+  float beta = R.f_beta;
+  if (R.field_mode && t + 1 < R.field_steps && a.maps)
+    beta = field_beta_f32(beta, R.f_field_eps, a.maps[R.map_base + (long long)b.clone * R.nodes + n]);
+  float P[9];
+  const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
+  if (!(drho > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const int ok = opp_of(k);
+    if (!gather || ((mask >> ok) & 1)) {
+      A[c0 + ok] = P[k];
+    } else {
+      const int cx = cx_of(k), cy = cy_of(k);
+      const int tx = cx == 1 ? (x == W - 1 ? 0 : x + 1) : (cx == -1 ? (x == 0 ? W - 1 : x - 1) : x);
+      const int ty = y + cy;
+      if (ty < 0 || ty >= H) continue;
+      if (tx > R.xmin && tx < R.xmax && ty > R.ymin && ty < R.ymax) continue;  // into the square
+      const int txc = cx == 1 ? cp : (cx == -1 ? cm : c0);
+      const int tl = ly + cy;
+      float *base = tl < 0 ? b.prev : (tl >= rows ? b.next : A);
+      const int roff = tl < 0 ? (rows - 1 - ly) * rowstep : (tl >= rows ? -ly * rowstep : cy * rowstep);
+      base[txc + roff + k] = P[k];
+    }
+  }
+}
+
+__device__ __forceinline__ Band make_band(const TemporalArgs &a, float *A, cg::cluster_group &cluster) {
+  Band b;
+  b.cs = (int)cluster.num_blocks();
+  b.rank = (int)cluster.block_rank();
+  b.clone = blockIdx.x / b.cs;
+  b.W = a.rd.W;
+  b.H = a.rd.H;
+  b.rows = b.H / b.cs;
+  b.row0 = b.rank * b.rows;
+  b.nb = b.rows * b.W;
+  b.rowstep = b.W * 9;
+  b.prev = b.rank > 0 ? cluster.map_shared_rank(A, b.rank - 1) : A;
+  b.next = b.rank + 1 < b.cs ? cluster.map_shared_rank(A, b.rank + 1) : A;
+  b.plane = a.rd.plane;
+  const long long cb = a.rd.pop_base + (long long)b.clone * 9 * b.plane;
+  b.src = a.src + cb;
+  b.dst = a.dst + cb;
+  return b;
+}
+
+// P_0 into the "after a local step" layout A[node*9 + opp k]
+template <int THREADS>
+__device__ __forceinline__ void load_band(const Band &b, float *A) {
+  for (int i = threadIdx.x; i < b.nb; i += THREADS) {
+    const long long n = (long long)b.row0 * b.W + i;
+#pragma unroll
+    for (int k = 0; k < 9; k++) A[i * 9 + opp_of(k)] = b.src[k * b.plane + n];
+  }
+}
+
+// One node away from the walls and the square, not the last step of the
+// interval.  C, U, D = the node's row and the rows above (y-1) and below
+// (y+1); om, o0, op = the column offsets of x-1, x, x+1 (times 9).  GATHER:
+// S(n,k) = A[n - c_k][opp k], P(n,k) -> A[n + c_k][k]; local step: S(n,k) =
+// A[n][k], P(n,k) -> A[n][opp k].  FIELD: beta scaled by (1 + feps * map[0]),
+// feps = 0 once the field's steps are over (field_beta_f32 then returns beta
+// exactly).  A density at or below zero sets `bad`.
+template <bool GATHER, bool FIELD>
+__device__ __forceinline__ void update_fast(const RunDev &R, float *C, float *U, float *D, int om, int o0,
+                                            int op, const float *map, float feps, bool &bad) {
+  float S[9];
+  if (GATHER) {
+    S[0] = C[o0 + 0];
+    S[1] = C[om + 3];
+    S[3] = C[op + 1];
+    S[2] = U[o0 + 4];
+    S[5] = U[om + 7];
+    S[6] = U[op + 8];
+    S[4] = D[o0 + 2];
+    S[7] = D[op + 5];
+    S[8] = D[om + 6];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; k++) S[k] = C[o0 + k];
+  }
+  float beta = R.f_beta;
+  if (FIELD) beta = field_beta_f32(beta, feps, map[0]);
+  float P[9];
+  const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
+  bad |= !(drho > -1.0f);
+  if (GATHER) {
+    C[o0 + 0] = P[0];
+    C[op + 1] = P[1];
+    C[om + 3] = P[3];
+    D[o0 + 2] = P[2];
+    D[op + 5] = P[5];
+    D[om + 6] = P[6];
+    U[o0 + 4] = P[4];
+    U[om + 7] = P[7];
+    U[op + 8] = P[8];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; k++) C[o0 + opp_of(k)] = P[k];
+  }
+}
+
+// Bit j set: the whole warp's node slot j is away from walls, the square and
+// band edges, so all neighbours are in this CTA and nothing bounces back.
+// (Measured: a separate band-edge path through distributed shared memory and
+// a wider class for the local steps were both slower than sending those rows
+// through update_general.)
+__device__ __forceinline__ void classify(unsigned &bulk, int j, bool pad, const RunDev &R, const Band &b,
+                                         int x, int ly) {
+  const int y = b.row0 + ly;
+  const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+  const bool wall = y == 0 || y == b.H - 1;
+  const bool edge = b.cs > 1 && (ly == 0 || ly == b.rows - 1);
+  if (__all_sync(0xffffffffu, pad || !(in_box || wall || edge))) bulk |= 1u << j;
+}
+
+__device__ __forceinline__ float field_eps(const TemporalArgs &a, int t) {
+  return t + 1 < a.rd.field_steps ? a.rd.f_field_eps : 0.0f;
+}
+
+// Generic kernel: any W; nodes i = tid + j*THREADS.
+template <int THREADS, int MINB, bool FIELD>
 __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) {
   // A[node * 9 + k]: a node's nine values together (stride 9 words: no bank
   // conflicts across a warp), so every access is a base register plus an
   // immediate offset
   extern __shared__ float A[];
   cg::cluster_group cluster = cg::this_cluster();
-  const int cs = (int)cluster.num_blocks();
-  const int rank = (int)cluster.block_rank();
+  const Band b = make_band(a, A, cluster);
   const RunDev &R = a.rd;
-  const int clone = blockIdx.x / cs;
-  const int W = R.W, H = R.H;
-  const int rows = H / cs, row0 = rank * rows;
-  const int nb = rows * W;
-  float *prev = rank > 0 ? cluster.map_shared_rank(A, rank - 1) : A;
-  float *next = rank + 1 < cs ? cluster.map_shared_rank(A, rank + 1) : A;
-  const long long plane = R.plane;
-  const long long cb = R.pop_base + (long long)clone * 9 * plane;
-  const float *src = a.src + cb;
-  float *dst = a.dst + cb;
-  // P_0 into the "after a local step" layout
-  for (int i = threadIdx.x; i < nb; i += THREADS) {
-    const long long n = (long long)row0 * W + i;
-#pragma unroll
-    for (int k = 0; k < 9; k++) A[i * 9 + opp_of(k)] = src[k * plane + n];
-  }
-  // bulk[j]: the whole warp's node j is away from band edges, walls and the
-  // square, so all its neighbours are in this CTA and nothing bounces back
-  const int npt = (nb + THREADS - 1) / THREADS;
-  unsigned bulk_bits = 0;
+  load_band<THREADS>(b, A);
+  const int npt = (b.nb + THREADS - 1) / THREADS;
+  unsigned bulk = 0;
   for (int j = 0; j < npt && j < 32; j++) {
     const int i = threadIdx.x + j * THREADS;
-    const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = row0 + ly;
-    const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
-    const bool ok = i >= nb || !(in_box || y == 0 || y == H - 1 || (cs > 1 && (ly == 0 || ly == rows - 1)));
-    if (__all_sync(0xffffffffu, ok)) bulk_bits |= 1u << j;
+    const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
+    classify(bulk, j, i >= b.nb, R, b, x, ly);
   }
-  const int rowstep = W * 9;  // one row in A, in words
+  const float *map = FIELD ? a.maps + R.map_base + (long long)b.clone * R.nodes + (long long)b.row0 * b.W : nullptr;
+  bool bad = false;
   cluster.sync();
-  for (int t = 0; t < a.steps; t++) {
-    const bool gather = (t & 1) == 0, last = t == a.steps - 1;
+  // every step but the last: warp-uniform bulk rows through update_fast
+  // (GATHER known at compile time), the rest through update_general
+  for (int t = 0; t + 1 < a.steps; t++) {
+    const bool gather = (t & 1) == 0;
+    const float feps = FIELD ? field_eps(a, t) : 0.0f;
     float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
     for (int j = 0; j < npt; j++) {
       const int i = threadIdx.x + j * THREADS;
-      if (i >= nb) continue;
-      const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = row0 + ly;
-      const bool bulk = j < 32 && ((bulk_bits >> j) & 1u);
-      // source / target columns: x-1 and x+1 with the periodic wrap
-      const int cm = (x == 0 ? i + W - 1 : i - 1) * 9;
-      const int c0 = i * 9;
-      const int cp = (x == W - 1 ? i - (W - 1) : i + 1) * 9;
-      float S[9];
-      int mask = 0;
-      bool in_box = false;
-      if (bulk) {
-        if (gather) {
-          // S(n,k) = A[n - c_k][opp k]
-          S[0] = A[c0 + 0];
-          S[1] = A[cm + 3];
-          S[2] = A[c0 - rowstep + 4];
-          S[3] = A[cp + 1];
-          S[4] = A[c0 + rowstep + 2];
-          S[5] = A[cm - rowstep + 7];
-          S[6] = A[cp - rowstep + 8];
-          S[7] = A[cp + rowstep + 5];
-          S[8] = A[cm + rowstep + 6];
-        } else {
-#pragma unroll
-          for (int k = 0; k < 9; k++) S[k] = A[c0 + k];
-        }
-      } else {
-        in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
-        mask = (in_box || y == 0 || y == H - 1) ? bounce_mask(R, x, y) : 0;
-        if (mask & 512) {  // inside the square
-          if (last) {
-            const long long n = (long long)y * W + x;
-#pragma unroll
-            for (int k = 0; k < 9; k++) dst[k * plane + n] = 0.0f;
-          }
-          continue;
-        }
-#pragma unroll
-        for (int k = 0; k < 9; k++) {
-          if (!gather || ((mask >> k) & 1)) {
-            S[k] = A[c0 + k];
-          } else {
-            const int cx = cx_of(k), cy = cy_of(k);
-            const int sxc = cx == 1 ? cm : (cx == -1 ? cp : c0);  // column, row ly
-            const int sl = ly - cy;                                 // source row, band-local
-            const float *base = sl < 0 ? prev : (sl >= rows ? next : A);
-            const int roff = sl < 0 ? (rows - 1 - ly) * rowstep : (sl >= rows ? -ly * rowstep : -cy * rowstep);
-            S[k] = base[sxc + roff + opp_of(k)];
-          }
-        }
-        if (in_box) store_drag_terms<false>(R, S, x, y, clone, terms);
-      }
-      if (last) {
-        const long long n = (long long)y * W + x;
-        float d = 0.f;
-#pragma unroll
-        for (int k = 0; k < 9; k++) {
-          dst[k * plane + n] = S[k];
-          d += S[k];
-        }
-        if (!(d > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
+      if (i >= b.nb) continue;
+      if (!(j < 32 && ((bulk >> j) & 1u))) {
+        update_general(a, b, A, i, t, gather, false, terms);
         continue;
       }
-      float beta = R.f_beta;
-      if (R.field_mode && t + 1 < R.field_steps && a.maps)
-        beta *= 1.0f + R.f_field_eps * a.maps[R.map_base + (long long)clone * R.nodes + (long long)y * W + x];
-      float P[9];
-      const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
-      if (!(drho > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
-      if (bulk) {
-        if (gather) {
-          // P(n,k) -> A[n + c_k][k]
-          A[c0 + 0] = P[0];
-          A[cp + 1] = P[1];
-          A[c0 + rowstep + 2] = P[2];
-          A[cm + 3] = P[3];
-          A[c0 - rowstep + 4] = P[4];
-          A[cp + rowstep + 5] = P[5];
-          A[cm + rowstep + 6] = P[6];
-          A[cm - rowstep + 7] = P[7];
-          A[cp - rowstep + 8] = P[8];
-        } else {
-#pragma unroll
-          for (int k = 0; k < 9; k++) A[c0 + opp_of(k)] = P[k];
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < 9; k++) {
-          const int ok = opp_of(k);
-          if (!gather || ((mask >> ok) & 1)) {
-            A[c0 + ok] = P[k];
-          } else {
-            const int cx = cx_of(k), cy = cy_of(k);
-            const int tx = cx == 1 ? (x == W - 1 ? 0 : x + 1) : (cx == -1 ? (x == 0 ? W - 1 : x - 1) : x);
-            const int ty = y + cy;
-            if (ty < 0 || ty >= H) continue;
-            if (tx > R.xmin && tx < R.xmax && ty > R.ymin && ty < R.ymax) continue;  // into the square
-            const int txc = cx == 1 ? cp : (cx == -1 ? cm : c0);
-            const int tl = ly + cy;
-            float *base = tl < 0 ? prev : (tl >= rows ? next : A);
-            const int roff = tl < 0 ? (rows - 1 - ly) * rowstep : (tl >= rows ? -ly * rowstep : cy * rowstep);
-            base[txc + roff + k] = P[k];
-          }
-        }
-      }
+      const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
+      const int o0 = x * 9, om = (x == 0 ? b.W - 1 : x - 1) * 9, op = (x == b.W - 1 ? 0 : x + 1) * 9;
+      float *C = A + ly * b.rowstep;
+      if (gather)
+        update_fast<true, FIELD>(R, C, C - b.rowstep, C + b.rowstep, om, o0, op, map + i, feps, bad);
+      else
+        update_fast<false, FIELD>(R, C, C - b.rowstep, C + b.rowstep, om, o0, op, map + i, feps, bad);
     }
     cluster.sync();
   }
+  // the last step stores S_T (one step in T: every node through update_general)
+  {
+    const int t = a.steps - 1;
+    float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
+    for (int i = threadIdx.x; i < b.nb; i += THREADS) update_general(a, b, A, i, t, (t & 1) == 0, true, terms);
+  }
+  if (bad) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
+  cluster.sync();  // no CTA leaves while a neighbour may still read its shared memory
 }
+
+// Fixed-column kernel: W divides THREADS, so each thread owns one column x
+// and the rows ly0 + j*(THREADS/W), j < NPT; every shared-memory address of
+// the bulk path is a loop-invariant per-thread base register plus a
+// compile-time offset.
+template <int THREADS, int NPT, bool GATHER, bool FIELD>
+__device__ __forceinline__ void bulk_rows(const RunDev &R, float *C0, int rowstep, int om, int o0, int op,
+                                          const float *map0, float feps, unsigned bulk, bool &bad) {
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    if (!((bulk >> j) & 1u)) continue;
+    float *C = C0 + j * THREADS * 9;
+    update_fast<GATHER, FIELD>(R, C, C - rowstep, C + rowstep, om, o0, op, map0 + j * THREADS, feps, bad);
+  }
+}
+
+template <int THREADS, int NPT, bool FIELD>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_temporal_f32_fixed(TemporalArgs a) {
+  extern __shared__ float A[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const Band b = make_band(a, A, cluster);
+  const RunDev &R = a.rd;
+  load_band<THREADS>(b, A);
+  const int x = threadIdx.x % b.W, ly0 = threadIdx.x / b.W;
+  const int rpj = THREADS / b.W;  // rows per slot j
+  const int o0 = x * 9, om = (x == 0 ? b.W - 1 : x - 1) * 9, op = (x == b.W - 1 ? 0 : x + 1) * 9;
+  unsigned bulk = 0;
+#pragma unroll
+  for (int j = 0; j < NPT; j++) classify(bulk, j, false, R, b, x, ly0 + j * rpj);
+  const float *map0 =
+      FIELD ? a.maps + R.map_base + (long long)b.clone * R.nodes + (long long)b.row0 * b.W + threadIdx.x : nullptr;
+  float *C0 = A + ly0 * b.rowstep;
+  bool bad = false;
+  cluster.sync();
+  for (int t = 0; t + 1 < a.steps; t++) {
+    const float feps = FIELD ? field_eps(a, t) : 0.0f;
+    const bool gather = (t & 1) == 0;
+    if (gather)
+      bulk_rows<THREADS, NPT, true, FIELD>(R, C0, b.rowstep, om, o0, op, map0, feps, bulk, bad);
+    else
+      bulk_rows<THREADS, NPT, false, FIELD>(R, C0, b.rowstep, om, o0, op, map0, feps, bulk, bad);
+    // band-edge rows and rows with walls or the square: one copy of the
+    // general update, not unrolled.  Within a step every node reads and
+    // writes only its own slots of A, so the order of the loops does not
+    // matter.
+    float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
+#pragma unroll 1
+    for (int j = 0; j < NPT; j++)
+      if (!((bulk >> j) & 1u)) update_general(a, b, A, threadIdx.x + j * THREADS, t, gather, false, terms);
+    cluster.sync();
+  }
+  {
+    const int t = a.steps - 1;
+    float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
+#pragma unroll 1
+    for (int j = 0; j < NPT; j++) update_general(a, b, A, threadIdx.x + j * THREADS, t, (t & 1) == 0, true, terms);
+  }
+  if (bad) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
+  cluster.sync();
+}
+
+typedef void (*TemporalFn)(TemporalArgs);
 
 struct TemporalVariant {
   int threads;
-  void (*fn)(TemporalArgs);
+  bool fixed;
+  TemporalFn fn[2];           // [field]
+  TemporalFn fixed_fn[2][4];  // [field][NPT = 1, 2, 4, 8]
 };
 
+#define FIXED1(T, F) \
+  {k_temporal_f32_fixed<T, 1, F>, k_temporal_f32_fixed<T, 2, F>, k_temporal_f32_fixed<T, 4, F>, k_temporal_f32_fixed<T, 8, F>}
+#define FIXED(T) {FIXED1(T, false), FIXED1(T, true)}
+#define GENERIC(T, M) {k_temporal_f32<T, M, false>, k_temporal_f32<T, M, true>}
 static const TemporalVariant kTemporal[] = {
-    {1024, k_temporal_f32<1024, 1>}, {512, k_temporal_f32<512, 2>}, {256, k_temporal_f32<256, 4>}};
+    {1024, false, GENERIC(1024, 1), {}}, {512, false, GENERIC(512, 2), {}}, {256, false, GENERIC(256, 4), {}},
+    {1024, true, {}, FIXED(1024)},       {512, true, {}, FIXED(512)},       {256, true, {}, FIXED(256)}};
+#undef GENERIC
+#undef FIXED
+#undef FIXED1
 
 int temporal_variant_count() { return (int)(sizeof(kTemporal) / sizeof(kTemporal[0])); }
 
-// Launch one run's interval with cluster size cs (H % cs == 0); returns
-// cudaErrorInvalidConfiguration when the band does not fit in shared memory.
-cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W, int H,
-                            cudaStream_t s) {
-  if (variant < 0 || variant >= temporal_variant_count() || cs < 1 || H % cs) return cudaErrorInvalidValue;
+// the kernel of a variant for this band shape, or nullptr when it cannot run it
+static TemporalFn temporal_fn(int variant, int cs, int W, int H, bool field) {
+  if (variant < 0 || variant >= temporal_variant_count() || cs < 1 || H % cs) return nullptr;
   const TemporalVariant &v = kTemporal[variant];
   const size_t smem = sizeof(float) * 9 * (size_t)(H / cs) * W;
-  if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
-  cudaError_t e = cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  if (cs > 8) {
-    e = cudaFuncSetAttribute(v.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
+  if (smem > 227 * 1024) return nullptr;
+  if (!v.fixed) return v.fn[field];
+  if (v.threads % W) return nullptr;
+  const int nb = (H / cs) * W;
+  if (nb % v.threads) return nullptr;
+  switch (nb / v.threads) {
+    case 1: return v.fixed_fn[field][0];
+    case 2: return v.fixed_fn[field][1];
+    case 4: return v.fixed_fn[field][2];
+    case 8: return v.fixed_fn[field][3];
+    default: return nullptr;
   }
+}
+
+static cudaLaunchConfig_t temporal_config(int cs, int variant, int nclones, size_t smem, cudaStream_t s,
+                                          cudaLaunchAttribute *attr) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cs * nclones);
-  cfg.blockDim = dim3(v.threads);
+  cfg.blockDim = dim3(kTemporal[variant].threads);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = cs;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, v.fn, a);
+  return cfg;
+}
+
+static cudaError_t prepare(TemporalFn fn, int cs, size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && cs > 8) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
+}
+
+// Launch one run's interval with cluster size cs (H % cs == 0).
+cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W, int H,
+                            cudaStream_t s) {
+  const bool field = a.rd.field_mode != 0 && a.maps != nullptr;
+  TemporalFn fn = temporal_fn(variant, cs, W, H, field);
+  if (!fn || a.steps < 1) return cudaErrorInvalidConfiguration;
+  const size_t smem = sizeof(float) * 9 * (size_t)(H / cs) * W;
+  cudaError_t e = prepare(fn, cs, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = temporal_config(cs, variant, nclones, smem, s, attr);
+  return cudaLaunchKernelEx(&cfg, fn, a);
 }
 
 // Whether the cluster shape can be resident at all (occupancy query, no launch).
-int temporal_max_clusters(int cs, int variant, int W, int H) {
-  if (variant < 0 || variant >= temporal_variant_count() || cs < 1 || H % cs) return 0;
-  const TemporalVariant &v = kTemporal[variant];
+int temporal_max_clusters(int cs, int variant, int W, int H, bool field) {
+  TemporalFn fn = temporal_fn(variant, cs, W, H, field);
+  if (!fn) return 0;
   const size_t smem = sizeof(float) * 9 * (size_t)(H / cs) * W;
-  if (smem > 227 * 1024) return 0;
-  if (cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return 0;
-  if (cs > 8 && cudaFuncSetAttribute(v.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
-    return 0;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(cs * 64);
-  cfg.blockDim = dim3(v.threads);
-  cfg.dynamicSmemBytes = smem;
+  if (prepare(fn, cs, smem) != cudaSuccess) return 0;
   cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = cs;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cudaLaunchConfig_t cfg = temporal_config(cs, variant, 64, smem, nullptr, attr);
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, (void *)v.fn, &cfg) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveClusters(&n, (void *)fn, &cfg) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
