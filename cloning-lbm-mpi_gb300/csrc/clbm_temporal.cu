@@ -202,37 +202,70 @@ __device__ __forceinline__ float field_eps(const TemporalArgs &a, int t) {
   return t + 1 < a.rd.field_steps ? a.rd.f_field_eps : 0.0f;
 }
 
-// Generic kernel: any W; nodes i = tid + j*THREADS.
+// Shared memory of one CTA: the band's populations, then (generic kernel)
+// the segment list and one class byte per 32-node segment.
+__host__ __device__ inline size_t temporal_smem(int nb) {
+  const int nseg = (nb + 31) / 32;
+  return sizeof(float) * 9 * (size_t)nb + 2 * (size_t)((nseg + 7) & ~7) + (size_t)((nseg + 15) & ~15) + 16;
+}
+
+// Generic kernel: any W.  The band's nodes form 32-node segments; segments
+// that need update_general (walls, band edges, the square's box) cost several
+// times a bulk segment, so they are dealt out first, one per warp, and the
+// bulk segments fill in after them: entry k of the list goes to warp k % NW.
+// The step time is that of the slowest warp (every step ends at a cluster
+// barrier), which this keeps near the mean.
 template <int THREADS, int MINB, bool FIELD>
 __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) {
   // A[node * 9 + k]: a node's nine values together (stride 9 words: no bank
   // conflicts across a warp), so every access is a base register plus an
   // immediate offset
   extern __shared__ float A[];
+  constexpr int NW = THREADS / 32;
   cg::cluster_group cluster = cg::this_cluster();
   const Band b = make_band(a, A, cluster);
   const RunDev &R = a.rd;
   load_band<THREADS>(b, A);
-  const int npt = (b.nb + THREADS - 1) / THREADS;
-  unsigned bulk = 0;
-  for (int j = 0; j < npt && j < 32; j++) {
-    const int i = threadIdx.x + j * THREADS;
+  const int nseg = (b.nb + 31) / 32;
+  unsigned short *list = (unsigned short *)(A + (size_t)9 * b.nb);
+  unsigned char *general = (unsigned char *)(list + ((nseg + 7) & ~7));
+  int *ngen_s = (int *)(general + ((nseg + 15) & ~15));
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  for (int sg = warp; sg < nseg; sg += NW) {
+    const int i = sg * 32 + lane;
     const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
-    classify(bulk, j, i >= b.nb, R, b, x, ly);
+    unsigned bulk = 0;
+    classify(bulk, 0, i >= b.nb, R, b, x, ly);
+    if (lane == 0) general[sg] = bulk ? 0 : 1;
   }
+  __syncthreads();
+  if (warp == 0) {  // the list: general segments, then bulk ones
+    const unsigned lower = (1u << lane) - 1u;
+    int n = 0;
+    for (int pass = 1; pass >= 0; pass--)
+      for (int c = 0; c < nseg; c += 32) {
+        const bool take = c + lane < nseg && general[c + lane] == pass;
+        const unsigned m = __ballot_sync(0xffffffffu, take);
+        if (take) list[n + __popc(m & lower)] = (unsigned short)(c + lane);
+        n += __popc(m);
+        if (pass == 1 && lane == 0 && c + 32 >= nseg) *ngen_s = n;
+      }
+  }
+  __syncthreads();
+  const int ngen = *ngen_s;
   const float *map = FIELD ? a.maps + R.map_base + (long long)b.clone * R.nodes + (long long)b.row0 * b.W : nullptr;
   bool bad = false;
   cluster.sync();
-  // every step but the last: warp-uniform bulk rows through update_fast
-  // (GATHER known at compile time), the rest through update_general
+  // every step but the last: bulk segments through update_fast (GATHER known
+  // at compile time), the rest through update_general
   for (int t = 0; t + 1 < a.steps; t++) {
     const bool gather = (t & 1) == 0;
     const float feps = FIELD ? field_eps(a, t) : 0.0f;
     float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
-    for (int j = 0; j < npt; j++) {
-      const int i = threadIdx.x + j * THREADS;
+    for (int k = warp; k < nseg; k += NW) {
+      const int i = list[k] * 32 + lane;
       if (i >= b.nb) continue;
-      if (!(j < 32 && ((bulk >> j) & 1u))) {
+      if (k < ngen) {
         update_general(a, b, A, i, t, gather, false, terms);
         continue;
       }
@@ -342,7 +375,7 @@ int temporal_variant_count() { return (int)(sizeof(kTemporal) / sizeof(kTemporal
 static TemporalFn temporal_fn(int variant, int cs, int W, int H, bool field) {
   if (variant < 0 || variant >= temporal_variant_count() || cs < 1 || H % cs) return nullptr;
   const TemporalVariant &v = kTemporal[variant];
-  const size_t smem = sizeof(float) * 9 * (size_t)(H / cs) * W;
+  const size_t smem = temporal_smem((H / cs) * W);
   if (smem > 227 * 1024) return nullptr;
   if (!v.fixed) return v.fn[field];
   if (v.threads % W) return nullptr;
@@ -385,7 +418,7 @@ cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclo
   const bool field = a.rd.field_mode != 0 && a.maps != nullptr;
   TemporalFn fn = temporal_fn(variant, cs, W, H, field);
   if (!fn || a.steps < 1) return cudaErrorInvalidConfiguration;
-  const size_t smem = sizeof(float) * 9 * (size_t)(H / cs) * W;
+  const size_t smem = temporal_smem((H / cs) * W);
   cudaError_t e = prepare(fn, cs, smem);
   if (e != cudaSuccess) return e;
   cudaLaunchAttribute attr[1];
@@ -397,7 +430,7 @@ cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclo
 int temporal_max_clusters(int cs, int variant, int W, int H, bool field) {
   TemporalFn fn = temporal_fn(variant, cs, W, H, field);
   if (!fn) return 0;
-  const size_t smem = sizeof(float) * 9 * (size_t)(H / cs) * W;
+  const size_t smem = temporal_smem((H / cs) * W);
   if (prepare(fn, cs, smem) != cudaSuccess) return 0;
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = temporal_config(cs, variant, 64, smem, nullptr, attr);
