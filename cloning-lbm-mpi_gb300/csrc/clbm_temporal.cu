@@ -184,18 +184,14 @@ __device__ __forceinline__ void update_fast(const RunDev &R, float *C, float *U,
   }
 }
 
-// Bit j set: the whole warp's node slot j is away from walls, the square and
+// Whether the whole warp's 32-node segment is away from walls, the square and
 // band edges, so all neighbours are in this CTA and nothing bounces back.
-// (Measured: a separate band-edge path through distributed shared memory and
-// a wider class for the local steps were both slower than sending those rows
-// through update_general.)
-__device__ __forceinline__ void classify(unsigned &bulk, int j, bool pad, const RunDev &R, const Band &b,
-                                         int x, int ly) {
+__device__ __forceinline__ bool segment_is_bulk(bool pad, const RunDev &R, const Band &b, int x, int ly) {
   const int y = b.row0 + ly;
   const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
   const bool wall = y == 0 || y == b.H - 1;
   const bool edge = b.cs > 1 && (ly == 0 || ly == b.rows - 1);
-  if (__all_sync(0xffffffffu, pad || !(in_box || wall || edge))) bulk |= 1u << j;
+  return __all_sync(0xffffffffu, pad || !(in_box || wall || edge));
 }
 
 __device__ __forceinline__ float field_eps(const TemporalArgs &a, int t) {
@@ -214,7 +210,11 @@ __host__ __device__ inline size_t temporal_smem(int nb) {
 // times a bulk segment, so they are dealt out first, one per warp, and the
 // bulk segments fill in after them: entry k of the list goes to warp k % NW.
 // The step time is that of the slowest warp (every step ends at a cluster
-// barrier), which this keeps near the mean.
+// barrier), which this keeps near the mean.  (Measured on a 256x64 channel,
+// all slower than this: fast paths for band-edge and wall rows through
+// distributed shared memory, a cost-weighted water-filling of the bulk
+// segments over the warps, a fixed column per thread with compile-time
+// shared-memory offsets.)
 template <int THREADS, int MINB, bool FIELD>
 __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) {
   // A[node * 9 + k]: a node's nine values together (stride 9 words: no bank
@@ -234,8 +234,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
   for (int sg = warp; sg < nseg; sg += NW) {
     const int i = sg * 32 + lane;
     const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
-    unsigned bulk = 0;
-    classify(bulk, 0, i >= b.nb, R, b, x, ly);
+    const bool bulk = segment_is_bulk(i >= b.nb, R, b, x, ly);
     if (lane == 0) general[sg] = bulk ? 0 : 1;
   }
   __syncthreads();
@@ -289,105 +288,24 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
   cluster.sync();  // no CTA leaves while a neighbour may still read its shared memory
 }
 
-// Fixed-column kernel: W divides THREADS, so each thread owns one column x
-// and the rows ly0 + j*(THREADS/W), j < NPT; every shared-memory address of
-// the bulk path is a loop-invariant per-thread base register plus a
-// compile-time offset.
-template <int THREADS, int NPT, bool GATHER, bool FIELD>
-__device__ __forceinline__ void bulk_rows(const RunDev &R, float *C0, int rowstep, int om, int o0, int op,
-                                          const float *map0, float feps, unsigned bulk, bool &bad) {
-#pragma unroll
-  for (int j = 0; j < NPT; j++) {
-    if (!((bulk >> j) & 1u)) continue;
-    float *C = C0 + j * THREADS * 9;
-    update_fast<GATHER, FIELD>(R, C, C - rowstep, C + rowstep, om, o0, op, map0 + j * THREADS, feps, bad);
-  }
-}
-
-template <int THREADS, int NPT, bool FIELD>
-__global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_temporal_f32_fixed(TemporalArgs a) {
-  extern __shared__ float A[];
-  cg::cluster_group cluster = cg::this_cluster();
-  const Band b = make_band(a, A, cluster);
-  const RunDev &R = a.rd;
-  load_band<THREADS>(b, A);
-  const int x = threadIdx.x % b.W, ly0 = threadIdx.x / b.W;
-  const int rpj = THREADS / b.W;  // rows per slot j
-  const int o0 = x * 9, om = (x == 0 ? b.W - 1 : x - 1) * 9, op = (x == b.W - 1 ? 0 : x + 1) * 9;
-  unsigned bulk = 0;
-#pragma unroll
-  for (int j = 0; j < NPT; j++) classify(bulk, j, false, R, b, x, ly0 + j * rpj);
-  const float *map0 =
-      FIELD ? a.maps + R.map_base + (long long)b.clone * R.nodes + (long long)b.row0 * b.W + threadIdx.x : nullptr;
-  float *C0 = A + ly0 * b.rowstep;
-  bool bad = false;
-  cluster.sync();
-  for (int t = 0; t + 1 < a.steps; t++) {
-    const float feps = FIELD ? field_eps(a, t) : 0.0f;
-    const bool gather = (t & 1) == 0;
-    if (gather)
-      bulk_rows<THREADS, NPT, true, FIELD>(R, C0, b.rowstep, om, o0, op, map0, feps, bulk, bad);
-    else
-      bulk_rows<THREADS, NPT, false, FIELD>(R, C0, b.rowstep, om, o0, op, map0, feps, bulk, bad);
-    // band-edge rows and rows with walls or the square: one copy of the
-    // general update, not unrolled.  Within a step every node reads and
-    // writes only its own slots of A, so the order of the loops does not
-    // matter.
-    float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
-#pragma unroll 1
-    for (int j = 0; j < NPT; j++)
-      if (!((bulk >> j) & 1u)) update_general(a, b, A, threadIdx.x + j * THREADS, t, gather, false, terms);
-    cluster.sync();
-  }
-  {
-    const int t = a.steps - 1;
-    float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
-#pragma unroll 1
-    for (int j = 0; j < NPT; j++) update_general(a, b, A, threadIdx.x + j * THREADS, t, (t & 1) == 0, true, terms);
-  }
-  if (bad) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
-  cluster.sync();
-}
-
 typedef void (*TemporalFn)(TemporalArgs);
 
 struct TemporalVariant {
   int threads;
-  bool fixed;
-  TemporalFn fn[2];           // [field]
-  TemporalFn fixed_fn[2][4];  // [field][NPT = 1, 2, 4, 8]
+  TemporalFn fn[2];  // [field]
 };
 
-#define FIXED1(T, F) \
-  {k_temporal_f32_fixed<T, 1, F>, k_temporal_f32_fixed<T, 2, F>, k_temporal_f32_fixed<T, 4, F>, k_temporal_f32_fixed<T, 8, F>}
-#define FIXED(T) {FIXED1(T, false), FIXED1(T, true)}
 #define GENERIC(T, M) {k_temporal_f32<T, M, false>, k_temporal_f32<T, M, true>}
-static const TemporalVariant kTemporal[] = {
-    {1024, false, GENERIC(1024, 1), {}}, {512, false, GENERIC(512, 2), {}}, {256, false, GENERIC(256, 4), {}},
-    {1024, true, {}, FIXED(1024)},       {512, true, {}, FIXED(512)},       {256, true, {}, FIXED(256)}};
+static const TemporalVariant kTemporal[] = {{1024, GENERIC(1024, 1)}, {512, GENERIC(512, 2)}, {256, GENERIC(256, 4)}};
 #undef GENERIC
-#undef FIXED
-#undef FIXED1
 
 int temporal_variant_count() { return (int)(sizeof(kTemporal) / sizeof(kTemporal[0])); }
 
 // the kernel of a variant for this band shape, or nullptr when it cannot run it
 static TemporalFn temporal_fn(int variant, int cs, int W, int H, bool field) {
   if (variant < 0 || variant >= temporal_variant_count() || cs < 1 || H % cs) return nullptr;
-  const TemporalVariant &v = kTemporal[variant];
-  const size_t smem = temporal_smem((H / cs) * W);
-  if (smem > 227 * 1024) return nullptr;
-  if (!v.fixed) return v.fn[field];
-  if (v.threads % W) return nullptr;
-  const int nb = (H / cs) * W;
-  if (nb % v.threads) return nullptr;
-  switch (nb / v.threads) {
-    case 1: return v.fixed_fn[field][0];
-    case 2: return v.fixed_fn[field][1];
-    case 4: return v.fixed_fn[field][2];
-    case 8: return v.fixed_fn[field][3];
-    default: return nullptr;
-  }
+  if (temporal_smem((H / cs) * W) > 227 * 1024) return nullptr;
+  return kTemporal[variant].fn[field];
 }
 
 static cudaLaunchConfig_t temporal_config(int cs, int variant, int nclones, size_t smem, cudaStream_t s,

@@ -247,9 +247,8 @@ int clbm_profile_read(clbm_ctx *ctx, double *step_ms, int *nsteps);
  * step), then the cluster-resident interval kernel (every clone's populations
  * in the shared memory of one thread-block cluster for all the steps of an
  * interval, one launch per interval) for cluster sizes 1, 2, 4, 8, 16 and
- * six thread configurations (any width: 1024, 512, 256 threads; widths that
- * divide the thread count, with 1, 2, 4 or 8 rows a thread: 1024, 512, 256
- * threads), where the lattice fits.  At most 8 + 30 variants.  *best = chosen candidate,
+ * three thread counts (1024, 512, 256), where the lattice fits.  At most
+ * 8 + 15 variants.  *best = chosen candidate,
  * ms_per_variant (nullable, *nvariants entries, -1 = not runnable here) =
  * milliseconds per step.  With ms_per_variant NULL a result cached for the same
  * lattices and clone counts is reused.  FP64 contexts have one variant. */

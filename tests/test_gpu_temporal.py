@@ -10,7 +10,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 NSTREAM = 8   # streaming launch variants come first in the autotuner's numbering
-NTHREAD = 6   # thread configurations of the cluster-resident kernel (generic, fixed-column)
+NTHREAD = 3   # thread configurations of the cluster-resident kernel (1024, 512, 256)
 
 
 def temporal_variant(cs, tv=0):
@@ -19,11 +19,11 @@ def temporal_variant(cs, tv=0):
 
 @pytest.mark.parametrize("W,H,side,xc,yc,cs,tv,field", [
     (64, 24, 6, 16, 12, 1, 0, False),
-    (128, 32, 6, 32, 16, 2, 3, False),   # fixed-column kernel, 1024 threads, 2 rows per thread
-    (64, 32, 6, 20, 16, 2, 3, False),    # fixed-column, 1024 threads, 1 row per thread
-    (256, 16, 6, 64, 8, 2, 4, True),     # fixed-column, 512 threads, field
-    (64, 32, 6, 20, 16, 4, 5, False),    # fixed-column, 256 threads, 2 rows per thread
-    (32, 64, 5, 10, 30, 1, 5, False),    # fixed-column, one CTA, 8 rows per thread
+    (128, 32, 6, 32, 16, 2, 2, False),   # more box/edge segments (15) than warps of a CTA (8)
+    (64, 32, 6, 20, 16, 2, 0, False),
+    (256, 16, 6, 64, 8, 2, 1, True),
+    (64, 32, 6, 20, 16, 4, 2, False),
+    (32, 64, 5, 10, 30, 1, 2, False),
     (64, 24, 6, 16, 12, 2, 1, False),
     (64, 24, 6, 16, 12, 4, 2, False),
     (200, 32, 8, 50, 16, 4, 0, True),
