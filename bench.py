@@ -17,10 +17,11 @@ e2e        the same metric through the C ABI as a driver calls it: the initial
            populations loaded from pinned host memory in the reference's AoS
            FP64 layout, then per interval the drag series, labels, weights and
            R_t read back to the host.
-roofline   the dominant kernel (the stream-collide step): algorithmic bytes
+roofline   the dominant kernel (the stream-collide step, or the cluster-resident
+           interval kernel when the autotuner picks it): algorithmic bytes
            (72 B/LUP FP32, 144 B/LUP FP64: one read and one write of nine
-           populations) per launch / its mean duration, from CUDA event pairs
-           around the step launches inside the timed region.
+           populations) per step / its mean duration, from CUDA event pairs
+           around the step (or interval) launches inside the timed region.
 cpu_baseline the oracle's C port of the reference hot loop on this host's cores.
 """
 from __future__ import annotations
@@ -355,7 +356,21 @@ def main():
     step_s = step_ms / 1e3 / max(1, nsteps)
     achieved = bpl * nodes_total / step_s / 1e9
     peak, peak_kind = hbm_peak()
-    traffic = ncu_traffic(f"k_step_{'f32' if wl.precision == clbm.FP32 else 'f64'}_{args.workload}.md")
+    vinfo = clbm.describe_variant(best) if wl.precision == clbm.FP32 else \
+        {"kind": "streaming", "kernel": "k_step_f64", "variant": 0}
+    cluster = vinfo["kind"] == "cluster-resident"
+    # DRAM bytes per launch of the dominant kernel (one step for the streaming
+    # kernel, one interval of wl.steps steps for the cluster-resident one)
+    traffic = ncu_traffic(f"{vinfo['kernel']}_{args.workload}.md")
+    launches_per_interval = (len(wl.runs) if cluster else wl.steps) + 4
+    # the streaming step kernel's own roofline, from the autotuner's timing of
+    # its best launch variant on this workload (one launch per step)
+    stream_ref = None
+    if len(tune_ms) >= clbm.STREAM_VARIANTS:
+        sms = min(float(x) for x in tune_ms[:clbm.STREAM_VARIANTS] if x > 0)
+        sa = bpl * nodes_total / (sms / 1e3) / 1e9
+        stream_ref = {"kernel": "k_step_f32", "ms_per_step": sms, "achieved": sa, "frac": sa / peak,
+                      "traffic": ncu_traffic(f"k_step_f32_{args.workload}.md")}
 
     # ---- e2e: initial load from pinned host memory + per-interval host reads ----
     e2e = None
@@ -415,11 +430,19 @@ def main():
                          f"{nodes_total * 9 * (4 if wl.precision == clbm.FP32 else 8) / 1e9:.2f} GB)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "k_step", "bytes_per_lup": bpl,
-                     "mean_step_ms": step_ms / max(1, nsteps)},
+                     "kernel": vinfo["kernel"], "variant": vinfo, "bytes_per_lup": bpl,
+                     "mean_step_ms": step_ms / max(1, nsteps),
+                     **({"note": "cluster-resident interval kernel: each clone's populations stay in "
+                                 "the shared memory of one thread-block cluster for all the steps of "
+                                 "an interval, so DRAM traffic per launch (traffic, one interval) is "
+                                 "a small fraction of the 72 B/LUP a streaming step must move; "
+                                 "achieved counts those algorithmic bytes, hence frac > 1 = the gain "
+                                 "over the HBM roofline of streaming; the streaming step kernel's "
+                                 "own figures are under streaming_step",
+                         "streaming_step": stream_ref} if cluster else {})},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": (wl.steps + 4) * args.steps,
+        "gpu_launches": launches_per_interval * args.steps,
         "graph": bool(args.graph),
         "clocks": clocks,
         "rvalues_tail": [float(x) for x in rv[:, -1]],

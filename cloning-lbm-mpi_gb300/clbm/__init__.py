@@ -176,6 +176,23 @@ def ref_perturbed_state_noalloc(fin, snaps, eps, nsnap, n, prefactors: np.ndarra
 
 
 # ---- sampler level ----
+# Interval-kernel variant numbering of clbm_autotune / clbm_set_step_variant:
+# 0..7 the streaming step kernel's launch variants (one launch per step), then
+# the cluster-resident interval kernel for cluster sizes 1, 2, 4, 8, 16 times
+# thread counts 1024, 512, 256 (one launch per run per interval).
+STREAM_VARIANTS = 8
+TEMPORAL_THREADS = (1024, 512, 256)
+
+
+def describe_variant(v: int) -> dict:
+    if v < STREAM_VARIANTS:
+        return {"kind": "streaming", "kernel": "k_step_f32", "variant": v}
+    q = v - STREAM_VARIANTS
+    return {"kind": "cluster-resident", "kernel": "k_temporal_f32", "variant": v,
+            "cluster_size": 1 << (q // len(TEMPORAL_THREADS)),
+            "threads": TEMPORAL_THREADS[q % len(TEMPORAL_THREADS)]}
+
+
 class Sampler:
     """One clbm context: every clone of one or several runs on the device."""
 
