@@ -232,11 +232,12 @@ int clbm_intervals_done(clbm_ctx *ctx, int run, int *done);
  * (nullable, [nruns][intervals]) receives R_t of every interval. */
 int clbm_run_sampler(clbm_ctx *ctx, int steps, int intervals, double *rvalues);
 
-/* Timing of the step kernels: while enabled, every interval enqueued
+/* Timing of the interval kernels: while enabled, every interval enqueued
  * eagerly (run_interval, or run_sampler without CUDA graphs) records a CUDA
- * event pair around its step launches on the context's stream.  Enabling
+ * event pair around its LB steps on the context's stream (the T step
+ * launches, or the cluster-resident kernel's one launch per run).  Enabling
  * resets the accumulators; clbm_profile_read returns the summed milliseconds
- * and the number of step launches since then (and resets them). */
+ * and the number of LB steps they cover (and resets them). */
 int clbm_profile(clbm_ctx *ctx, int enable);
 int clbm_profile_read(clbm_ctx *ctx, double *step_ms, int *nsteps);
 
