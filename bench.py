@@ -117,14 +117,18 @@ def ncu_traffic(kernel_file: str):
 
 
 def dist_setup(args):
+    """One process per GPU under torchrun: NCCL for the GPU arm, gloo for the
+    reference arm (host cores only; rank 0 alone measures)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl" if args.impl != "reference" else "gloo")
+        gpu = args.impl != "reference"
+        if gpu:
+            torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if gpu else "gloo")
     return world, rank, local
 
 
@@ -135,11 +139,13 @@ def barrier(world):
 
 
 def allmax(world, x: float) -> float:
+    """Maximum of x over the ranks (the slowest rank's time)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

@@ -31,7 +31,7 @@ EXPORTS = [
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
-    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant",
+    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant", "clbm_shard_plan",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -111,6 +111,7 @@ def lib() -> C.CDLL:
         L.clbm_error_word.argtypes = [vp, C.POINTER(C.c_uint), i]
         L.clbm_sync.argtypes = [vp]
         L.clbm_stream.argtypes = [vp]
+        L.clbm_shard_plan.argtypes = [vp, i, i, i, vp, C.POINTER(i), vp, C.POINTER(i), vp, C.POINTER(i)]
         _lib = L
     return _lib
 
@@ -176,6 +177,19 @@ def ref_perturbed_state_noalloc(fin, snaps, eps, nsnap, n, prefactors: np.ndarra
 
 
 # ---- sampler level ----
+def shard_plan(labels: np.ndarray, nshards: int, shard: int) -> dict:
+    """clbm_shard_plan: this shard's sends, receives and local copies, each an
+    (n, 3) int array of (src_slot, dst_slot, peer) in ascending dst_slot."""
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    n = lab.size
+    out = {k: np.zeros((n, 3), dtype=np.int32) for k in ("sends", "recvs", "locals")}
+    cnt = {k: C.c_int() for k in out}
+    check(lib().clbm_shard_plan(_p(lab), n, nshards, shard, _p(out["sends"]), C.byref(cnt["sends"]),
+                                _p(out["recvs"]), C.byref(cnt["recvs"]), _p(out["locals"]),
+                                C.byref(cnt["locals"])), "clbm_shard_plan")
+    return {k: out[k][:cnt[k].value] for k in out}
+
+
 # Interval-kernel variant numbering of clbm_autotune / clbm_set_step_variant:
 # 0..7 the streaming step kernel's launch variants (one launch per step), then
 # the cluster-resident interval kernel for cluster sizes 1, 2, 4, 8, 16 times

@@ -303,6 +303,25 @@ int clbm_get_drag_grad_aos_f64(clbm_ctx *ctx, int run, int clone, double *aos);
 
 /* device error word (CLBM_DEV_* bits) accumulated since the last clear */
 int clbm_error_word(clbm_ctx *ctx, unsigned *word, int clear);
+/* ---- clones split over processes (one GPU each) ---------------------------
+ * Replaces the MPI clone exchange of the pops driver
+ * (src/mpi_LBM_GK_pops_perturb.cpp:650-699): clones in contiguous blocks of
+ * nclones / nshards per shard; after a cloning step slot j takes the state of
+ * slot labels[j] (labels[j] == j keeps it; a parent keeps its own state).
+ * For shard `shard` the plan lists (global slots, peer shard) the copies it
+ * sends, receives and does locally, each list in ascending destination slot
+ * (both ends of a transfer see it at the same position).  Any list pointer
+ * may be NULL (counts only); each holds at most nclones entries.  Host only:
+ * no device is needed. */
+typedef struct {
+  int src_slot; /* global index of the parent slot */
+  int dst_slot; /* global index of the slot that takes its state */
+  int peer;     /* the other shard (this shard for local copies) */
+} clbm_copy;
+int clbm_shard_plan(const int *labels, int nclones, int nshards, int shard,
+                    clbm_copy *sends, int *nsends, clbm_copy *recvs,
+                    int *nrecvs, clbm_copy *locals, int *nlocals);
+
 /* block until the context's stream is idle */
 int clbm_sync(clbm_ctx *ctx);
 /* the context's cudaStream_t */
