@@ -28,10 +28,28 @@ namespace cg = cooperative_groups;
 
 namespace clbm {
 
-// Geometry of one CTA's band, shared by both kernels.
+// Distributed shared memory through 32-bit shared::cluster addresses: the
+// address of this CTA's shared-memory offset `a` in the CTA of cluster rank
+// `rank`, and FP32 loads / stores at such addresses.
+__device__ __forceinline__ unsigned cluster_addr(unsigned a, int rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float ld_cluster(unsigned a) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_cluster(unsigned a, float v) {
+  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+
+// Geometry of one CTA's band.
 struct Band {
   int cs, rank, clone, W, H, rows, row0, nb, rowstep;
   float *prev, *next;
+  unsigned own_c, prev_c, next_c;  // shared::cluster byte addresses of A in this / previous / next CTA
   long long plane;
   const float *src;
   float *dst;
@@ -108,6 +126,88 @@ __device__ __forceinline__ void update_general(const TemporalArgs &a, const Band
   }
 }
 
+// update_general for a gather step that is not the last: every slot the node
+// reads is addressed once (32-bit shared::cluster address: this CTA, or the
+// neighbour CTA across a band edge), and P(n,k) goes back to the slot S(n,
+// opp k) came from -- the pull rules make the two the same slot (own slot opp
+// k when that slot bounces, else (n + c_k, k)) -- unless the target row lies
+// outside the channel or the target inside the square (the push is dropped,
+// as in update_general).
+__device__ __forceinline__ void update_general_gather(const TemporalArgs &a, const Band &b, int i, int t,
+                                                      bool &bad, float *terms) {
+  const RunDev &R = a.rd;
+  const int W = b.W, H = b.H, rows = b.rows, rs = b.rowstep;
+  const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = b.row0 + ly;
+  const int xm = x == 0 ? W - 1 : x - 1, xp = x == W - 1 ? 0 : x + 1;
+  const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+  const int mask = (in_box || y == 0 || y == H - 1) ? bounce_mask(R, x, y) : 0;
+  if (mask & 512) return;  // inside the square
+  // byte addresses of column 0 of the rows y-1, y, y+1
+  const unsigned rowC = b.own_c + 4u * (unsigned)(ly * rs);
+  const unsigned rowU = ly == 0 ? b.prev_c + 4u * (unsigned)((rows - 1) * rs) : rowC - 4u * (unsigned)rs;
+  const unsigned rowD = ly == rows - 1 ? b.next_c : rowC + 4u * (unsigned)rs;
+  const unsigned own = rowC + 36u * (unsigned)x;
+  unsigned ad[9];
+  float S[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    if ((mask >> k) & 1) {
+      ad[k] = own + 4u * k;
+    } else {  // S(n,k) = A[n - c_k][opp k]
+      const int cx = cx_of(k), cy = cy_of(k);
+      const int sx = cx == 1 ? xm : (cx == -1 ? xp : x);
+      const unsigned row = cy == 1 ? rowU : (cy == -1 ? rowD : rowC);
+      ad[k] = row + 36u * (unsigned)sx + 4u * opp_of(k);
+    }
+    S[k] = ld_cluster(ad[k]);
+  }
+  if (in_box) store_drag_terms<false>(R, S, x, y, b.clone, terms);
+  float beta = R.f_beta;
+  const long long n = (long long)y * W + x;
+  if (R.field_mode && t + 1 < R.field_steps && a.maps)
+    beta = field_beta_f32(beta, R.f_field_eps, a.maps[R.map_base + (long long)b.clone * R.nodes + n]);
+  float P[9];
+  const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
+  bad |= !(drho > -1.0f);
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const int ok = opp_of(k);
+    if (!((mask >> ok) & 1)) {
+      const int cx = cx_of(k), cy = cy_of(k);
+      const int tx = cx == 1 ? xp : (cx == -1 ? xm : x);
+      const int ty = y + cy;
+      if (ty < 0 || ty >= H) continue;
+      if (tx > R.xmin && tx < R.xmax && ty > R.ymin && ty < R.ymax) continue;  // into the square
+    }
+    st_cluster(ad[ok], P[k]);
+  }
+}
+
+// update_general for a local step that is not the last: the node swaps its
+// own slots; only the square's box needs more (drag terms, the interior).
+__device__ __forceinline__ void update_general_local(const TemporalArgs &a, const Band &b, float *A, int i,
+                                                     int t, bool &bad, float *terms) {
+  const RunDev &R = a.rd;
+  const int W = b.W;
+  const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = b.row0 + ly;
+  const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+  if (in_box && (bounce_mask(R, x, y) & 512)) return;  // inside the square
+  const int c0 = i * 9;
+  float S[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) S[k] = A[c0 + k];
+  if (in_box) store_drag_terms<false>(R, S, x, y, b.clone, terms);
+  float beta = R.f_beta;
+  const long long n = (long long)y * W + x;
+  if (R.field_mode && t + 1 < R.field_steps && a.maps)
+    beta = field_beta_f32(beta, R.f_field_eps, a.maps[R.map_base + (long long)b.clone * R.nodes + n]);
+  float P[9];
+  const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
+  bad |= !(drho > -1.0f);
+#pragma unroll
+  for (int k = 0; k < 9; k++) A[c0 + opp_of(k)] = P[k];
+}
+
 __device__ __forceinline__ Band make_band(const TemporalArgs &a, float *A, cg::cluster_group &cluster) {
   Band b;
   b.cs = (int)cluster.num_blocks();
@@ -121,6 +221,10 @@ __device__ __forceinline__ Band make_band(const TemporalArgs &a, float *A, cg::c
   b.rowstep = b.W * 9;
   b.prev = b.rank > 0 ? cluster.map_shared_rank(A, b.rank - 1) : A;
   b.next = b.rank + 1 < b.cs ? cluster.map_shared_rank(A, b.rank + 1) : A;
+  const unsigned a_cta = (unsigned)__cvta_generic_to_shared(A);
+  b.own_c = cluster_addr(a_cta, b.rank);
+  b.prev_c = b.rank > 0 ? cluster_addr(a_cta, b.rank - 1) : b.own_c;
+  b.next_c = b.rank + 1 < b.cs ? cluster_addr(a_cta, b.rank + 1) : b.own_c;
   b.plane = a.rd.plane;
   const long long cb = a.rd.pop_base + (long long)b.clone * 9 * b.plane;
   b.src = a.src + cb;
@@ -265,7 +369,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
       const int i = list[k] * 32 + lane;
       if (i >= b.nb) continue;
       if (k < ngen) {
-        update_general(a, b, A, i, t, gather, false, terms);
+        if (gather)
+          update_general_gather(a, b, i, t, bad, terms);
+        else
+          update_general_local(a, b, A, i, t, bad, terms);
         continue;
       }
       const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
