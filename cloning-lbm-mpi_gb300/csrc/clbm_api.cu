@@ -405,19 +405,55 @@ extern "C" int clbm_load_run_aos_f64(clbm_ctx *c, int run, const double *aos) {
   if (int s = check_run(c, run)) return s;
   if (!aos) return fail(CLBM_ERR_INVALID, "aos is NULL");
   const RunDev &R = c->runs_h[run];
-  const size_t n = 9 * (size_t)R.nodes;
-  const int chunk = (int)std::max<size_t>(1, std::min<size_t>(R.nclones, (size_t)(256u << 20) / (n * 8)));
-  double *stage = nullptr;
-  CK(cudaMallocAsync((void **)&stage, n * 8 * chunk, c->stream));
-  cudaError_t e = cudaSuccess;
-  for (int c0 = 0; c0 < R.nclones && e == cudaSuccess; c0 += chunk) {
-    const int m = std::min(chunk, R.nclones - c0);
-    e = cudaMemcpyAsync(stage, aos + (size_t)c0 * n, n * 8 * m, cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess)
-      e = launch_aos_to_soa(c->precision == CLBM_FP64, c->d.runs, run, c0, m, stage, c->pop[c->s_buf], c->stream);
+  const bool f64 = c->precision == CLBM_FP64;
+  const size_t n = 9 * (size_t)R.nodes, clone_bytes = n * 8;
+  // staging: the two halves of the population buffer that does not hold the
+  // current state (its content is dead until the next interval's reseed
+  // writes it), copies of chunk i+1 overlapping the conversion of chunk i
+  const size_t half = c->pop_elems * c->elem_size / 2;
+  const int chunk = (int)std::min<size_t>(R.nclones, half / clone_bytes);
+  if (chunk < 1) {  // one clone larger than half the buffer: a temporary stage
+    double *stage = nullptr;
+    CK(cudaMallocAsync((void **)&stage, clone_bytes, c->stream));
+    cudaError_t e = cudaSuccess;
+    for (int j = 0; j < R.nclones && e == cudaSuccess; j++) {
+      e = cudaMemcpyAsync(stage, aos + (size_t)j * n, clone_bytes, cudaMemcpyHostToDevice, c->stream);
+      if (e == cudaSuccess) e = launch_aos_to_soa(f64, c->d.runs, run, R.nodes, j, 1, stage, c->pop[c->s_buf], c->stream);
+    }
+    cudaFreeAsync(stage, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return clbm_status_from_cuda(e);
   }
-  cudaFreeAsync(stage, c->stream);
+  double *stage[2] = {(double *)c->pop[1 - c->s_buf],
+                      (double *)((char *)c->pop[1 - c->s_buf] + (half & ~(size_t)255))};
+  cudaStream_t conv = nullptr;
+  cudaEvent_t copied[2] = {nullptr, nullptr}, converted[2] = {nullptr, nullptr};
+  cudaError_t e = cudaStreamCreateWithFlags(&conv, cudaStreamNonBlocking);
+  for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+    e = cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&converted[b], cudaEventDisableTiming);
+  }
+  int i = 0;
+  for (int c0 = 0; c0 < R.nclones && e == cudaSuccess; c0 += chunk, i++) {
+    const int m = std::min(chunk, R.nclones - c0), b = i & 1;
+    if (i >= 2) e = cudaStreamWaitEvent(c->stream, converted[b], 0);  // chunk i-2 has left this half
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(stage[b], aos + (size_t)c0 * n, clone_bytes * m, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(copied[b], c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(conv, copied[b], 0);
+    if (e == cudaSuccess) e = launch_aos_to_soa(f64, c->d.runs, run, R.nodes, c0, m, stage[b], c->pop[c->s_buf], conv);
+    if (e == cudaSuccess) e = cudaEventRecord(converted[b], conv);
+  }
+  if (conv) {
+    const cudaError_t e2 = cudaStreamSynchronize(conv);
+    if (e == cudaSuccess) e = e2;
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  for (int b = 0; b < 2; b++) {
+    if (copied[b]) cudaEventDestroy(copied[b]);
+    if (converted[b]) cudaEventDestroy(converted[b]);
+  }
+  if (conv) cudaStreamDestroy(conv);
   return clbm_status_from_cuda(e);
 }
 
@@ -430,7 +466,7 @@ extern "C" int clbm_load_pops_aos_f64(clbm_ctx *c, int run, int clone, const dou
   CK(cudaMallocAsync((void **)&stage, n * 8, c->stream));
   cudaError_t e = cudaMemcpyAsync(stage, aos, n * 8, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess)
-    e = launch_aos_to_soa(c->precision == CLBM_FP64, c->d.runs, run, clone, 1, stage, c->pop[c->s_buf], c->stream);
+    e = launch_aos_to_soa(c->precision == CLBM_FP64, c->d.runs, run, R.nodes, clone, 1, stage, c->pop[c->s_buf], c->stream);
   cudaFreeAsync(stage, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return clbm_status_from_cuda(e);
@@ -447,7 +483,7 @@ extern "C" int clbm_dump_pops_aos_f64(clbm_ctx *c, int run, int clone, double *a
   const size_t n = 9 * (size_t)R.nodes;
   double *stage = nullptr;
   CK(cudaMallocAsync((void **)&stage, n * 8, c->stream));
-  cudaError_t e = launch_soa_to_aos(c->precision == CLBM_FP64, c->d.runs, run, parent, c->pop[c->s_buf], stage, c->stream);
+  cudaError_t e = launch_soa_to_aos(c->precision == CLBM_FP64, c->d.runs, run, R.nodes, parent, c->pop[c->s_buf], stage, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(aos, stage, n * 8, cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(stage, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -463,7 +499,7 @@ extern "C" int clbm_set_snapshots_aos_f64(clbm_ctx *c, int run, int nsnap, const
   double *stage = nullptr;
   CK(cudaMallocAsync((void **)&stage, n * 8, c->stream));
   cudaError_t e = cudaMemcpyAsync(stage, aos, n * 8, cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess) e = launch_snaps_to_soa(c->d.runs, run, nsnap, stage, c->d.snaps, c->stream);
+  if (e == cudaSuccess) e = launch_snaps_to_soa(c->d.runs, run, R.nodes, nsnap, stage, c->d.snaps, c->stream);
   cudaFreeAsync(stage, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e == cudaSuccess) c->snaps_loaded[run] = 1;
@@ -1044,7 +1080,7 @@ extern "C" int clbm_get_drag_grad_aos_f64(clbm_ctx *c, int run, int clone, doubl
   const size_t n = 9 * (size_t)R.nodes;
   double *stage = nullptr;
   CK(cudaMallocAsync((void **)&stage, n * 8, c->stream));
-  cudaError_t e = launch_soa_to_aos(c->precision == CLBM_FP64, c->d.runs, run, clone,
+  cudaError_t e = launch_soa_to_aos(c->precision == CLBM_FP64, c->d.runs, run, R.nodes, clone,
                                     c->adj.sig[c->adj.result], stage, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(aos, stage, n * 8, cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(stage, c->stream);

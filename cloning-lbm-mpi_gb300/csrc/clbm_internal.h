@@ -140,13 +140,13 @@ cudaError_t launch_scgf(const double *logr, int first, int count, double dT, dou
 cudaError_t launch_init_equilibrium(bool f64, const RunDev *runs, int nruns, int run, void *pop,
                                     double u0, double noise, unsigned long long seed, int blocks,
                                     cudaStream_t s);
-cudaError_t launch_aos_to_soa(bool f64, const RunDev *runs, int run, int clone0, int nclone,
+cudaError_t launch_aos_to_soa(bool f64, const RunDev *runs, int run, int nodes, int clone0, int nclone,
                               const double *aos, void *pop, cudaStream_t s);
-cudaError_t launch_soa_to_aos(bool f64, const RunDev *runs, int run, int clone, const void *pop,
+cudaError_t launch_soa_to_aos(bool f64, const RunDev *runs, int run, int nodes, int clone, const void *pop,
                               double *aos, cudaStream_t s);
 cudaError_t launch_macro(bool f64, const RunDev *runs, int run, int clone, int nodes, const void *pop,
                          double *rho, double *ux, double *uy, cudaStream_t s);
-cudaError_t launch_snaps_to_soa(const RunDev *runs, int run, int nsnap, const double *aos,
+cudaError_t launch_snaps_to_soa(const RunDev *runs, int run, int nodes, int nsnap, const double *aos,
                                 double *snaps, cudaStream_t s);
 
 }  // namespace clbm

@@ -557,18 +557,10 @@ cudaError_t launch_macro(bool f64, const RunDev *runs, int run, int clone, int n
   return cudaGetLastError();
 }
 
-static cudaError_t run_geometry(const RunDev *runs, int run, RunDev &h, cudaStream_t s) {
-  cudaError_t e = cudaMemcpyAsync(&h, runs + run, sizeof(RunDev), cudaMemcpyDeviceToHost, s);
-  if (e != cudaSuccess) return e;
-  return cudaStreamSynchronize(s);
-}
-
-cudaError_t launch_aos_to_soa(bool f64, const RunDev *runs, int run, int clone0, int nclone,
+// (nodes = W*H of the run, from the host copy of its descriptor)
+cudaError_t launch_aos_to_soa(bool f64, const RunDev *runs, int run, int nodes, int clone0, int nclone,
                               const double *aos, void *pop, cudaStream_t s) {
-  RunDev h;
-  cudaError_t e = run_geometry(runs, run, h, s);
-  if (e != cudaSuccess) return e;
-  dim3 grid((h.nodes + 255) / 256, nclone);
+  dim3 grid((nodes + 255) / 256, nclone);
   if (f64)
     k_aos_to_soa<true><<<grid, 256, 0, s>>>(runs, run, clone0, aos, pop);
   else
@@ -576,24 +568,18 @@ cudaError_t launch_aos_to_soa(bool f64, const RunDev *runs, int run, int clone0,
   return cudaGetLastError();
 }
 
-cudaError_t launch_soa_to_aos(bool f64, const RunDev *runs, int run, int clone, const void *pop,
+cudaError_t launch_soa_to_aos(bool f64, const RunDev *runs, int run, int nodes, int clone, const void *pop,
                               double *aos, cudaStream_t s) {
-  RunDev h;
-  cudaError_t e = run_geometry(runs, run, h, s);
-  if (e != cudaSuccess) return e;
   if (f64)
-    k_soa_to_aos<true><<<(h.nodes + 255) / 256, 256, 0, s>>>(runs, run, clone, pop, aos);
+    k_soa_to_aos<true><<<(nodes + 255) / 256, 256, 0, s>>>(runs, run, clone, pop, aos);
   else
-    k_soa_to_aos<false><<<(h.nodes + 255) / 256, 256, 0, s>>>(runs, run, clone, pop, aos);
+    k_soa_to_aos<false><<<(nodes + 255) / 256, 256, 0, s>>>(runs, run, clone, pop, aos);
   return cudaGetLastError();
 }
 
-cudaError_t launch_snaps_to_soa(const RunDev *runs, int run, int nsnap, const double *aos,
+cudaError_t launch_snaps_to_soa(const RunDev *runs, int run, int nodes, int nsnap, const double *aos,
                                 double *snaps, cudaStream_t s) {
-  RunDev h;
-  cudaError_t e = run_geometry(runs, run, h, s);
-  if (e != cudaSuccess) return e;
-  dim3 grid((h.nodes + 255) / 256, nsnap);
+  dim3 grid((nodes + 255) / 256, nsnap);
   k_snaps_to_soa<<<grid, 256, 0, s>>>(runs, run, aos, snaps);
   return cudaGetLastError();
 }
