@@ -807,6 +807,7 @@ extern "C" int clbm_profile_read(clbm_ctx *c, double *step_ms, int *nsteps) {
 // cluster-resident interval kernel's thread configurations.
 static void apply_variant(clbm_ctx *c, int v) {
   const int nv = step_variant_count();
+  const int cs0 = c->temporal_cs, sv0 = c->step_variant, tv0 = c->temporal_variant;
   if (v < nv) {
     c->step_variant = v;
     c->temporal_cs = 0;
@@ -815,6 +816,8 @@ static void apply_variant(clbm_ctx *c, int v) {
     c->temporal_cs = 1 << (q / temporal_variant_count());
     c->temporal_variant = q % temporal_variant_count();
   }
+  // captured intervals hold the previous variant's launches
+  if (c->temporal_cs != cs0 || c->step_variant != sv0 || c->temporal_variant != tv0) destroy_graphs(c);
 }
 
 // Autotuner: time every FP32 step variant on this context's own workload and

@@ -71,3 +71,31 @@ def test_autotune_considers_cluster_resident_kernel(gpu, clbm_lib, orc):
         assert np.array_equal(s.dump(0, 5), before)
         s.run_interval(20)
         assert s.error_word() == 0
+
+
+def test_graph_replay_with_cluster_resident_kernel(gpu, clbm_lib, orc):
+    """Intervals captured in CUDA graphs with the cluster-resident kernel (and
+    a switch of variant between captured intervals) equal eager streaming."""
+    g = orc.channel_geom(64, 24, 6, 16, 12)
+    u0, nc, T = 0.05, 5, 21
+    d = clbm_lib.RunDesc(width=g.nx, height=g.ny, xmin=g.xmin, xmax=g.xmax, ymin=g.ymin, ymax=g.ymax,
+                         nclones=nc, ranks=1, tau=0.57, beta=6 * u0 * u0 / (63 * 23), alpha=8.0,
+                         force_scale=2 / (u0 * u0 * 6), dt=u0 / 6, perturb_mode=clbm_lib.PERTURB_UNIFORM,
+                         eps=1e-4, seed=7)
+    with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T) as s:
+        s.set_step_variant(4)
+        s.init_equilibrium(0, u0, 1e-3, 7)
+        ref = s.run_sampler(T, 4)
+        ref_state = [s.dump(0, j) for j in range(nc)]
+    with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T, flags=clbm_lib.FLAG_GRAPH) as s:
+        s.set_step_variant(temporal_variant(2, 0))
+        s.init_equilibrium(0, u0, 1e-3, 7)
+        rv = [s.run_sampler(T, 2)]
+        s.set_step_variant(4)
+        rv.append(s.run_sampler(T, 1))
+        s.set_step_variant(temporal_variant(1, 1))
+        rv.append(s.run_sampler(T, 1))
+        assert s.error_word() == 0
+        assert np.array_equal(np.concatenate(rv, axis=1), ref)
+        for j in range(nc):
+            assert np.array_equal(s.dump(0, j), ref_state[j])
