@@ -31,7 +31,7 @@ EXPORTS = [
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
-    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant", "clbm_shard_plan",
+    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant", "clbm_shard_plan", "clbm_ref_random_field",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -112,6 +112,7 @@ def lib() -> C.CDLL:
         L.clbm_sync.argtypes = [vp]
         L.clbm_stream.argtypes = [vp]
         L.clbm_shard_plan.argtypes = [vp, i, i, i, vp, C.POINTER(i), vp, C.POINTER(i), vp, C.POINTER(i)]
+        L.clbm_ref_random_field.argtypes = [i, i, d, C.c_ulonglong, i, vp, C.POINTER(i)]
         _lib = L
     return _lib
 
@@ -177,6 +178,15 @@ def ref_perturbed_state_noalloc(fin, snaps, eps, nsnap, n, prefactors: np.ndarra
 
 
 # ---- sampler level ----
+def ref_random_field(dx: int, dy: int, sigma: float, seed: int, draw: int) -> tuple[np.ndarray, int]:
+    """clbm_ref_random_field: (map in the reference order y + dy*x, number of
+    clamped negative eigenvalues)."""
+    out = np.empty(dx * dy)
+    neg = C.c_int()
+    check(lib().clbm_ref_random_field(dx, dy, sigma, seed, draw, _p(out), C.byref(neg)), "clbm_ref_random_field")
+    return out, neg.value
+
+
 def shard_plan(labels: np.ndarray, nshards: int, shard: int) -> dict:
     """clbm_shard_plan: this shard's sends, receives and local copies, each an
     (n, 3) int array of (src_slot, dst_slot, peer) in ascending dst_slot."""

@@ -7,6 +7,7 @@
 // pending labels/marks say which parent each slot copies and which slots are
 // perturbed when the next interval starts.
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -1181,4 +1182,43 @@ extern "C" int clbm_get_field_map(clbm_ctx *c, int run, int clone, double *map, 
   for (int x = 0; x < R.W; x++)
     for (int y = 0; y < R.H; y++) map[y + (size_t)R.H * x] = (double)f[(size_t)y * R.W + x];
   return CLBM_OK;
+}
+
+extern "C" int clbm_ref_random_field(int dx, int dy, double sigma, unsigned long long seed, int draw,
+                                     double *map, int *negative) {
+  if (dx < 3 || dy < 4 || dx > 1024 || dy > 1024 || !(sigma > 0) || draw < 0 || !map)
+    return fail(CLBM_ERR_INVALID, "clbm_ref_random_field: need 3 <= dx <= 1024, 4 <= dy <= 1024, sigma > 0, "
+                                  "draw >= 0, map != NULL");
+  // a one-clone context whose only use is its field tables and kernels (the
+  // square is a placeholder: nothing is stepped)
+  clbm_run_desc d{};
+  d.width = dx;
+  d.height = dy;
+  d.xmin = 0;
+  d.xmax = 1;
+  d.ymin = 1;
+  d.ymax = 2;
+  d.nclones = 1;
+  d.ranks = 1;
+  d.tau = 1.0;
+  d.dt = 1.0;
+  d.force_scale = 1.0;
+  d.seed = seed;
+  d.field_mode = 1;
+  d.field_steps = 1;
+  d.field_eps = 1.0;
+  d.field_sigma = sigma;
+  clbm_ctx *c = nullptr;
+  if (int st = clbm_create(&d, 1, CLBM_FP32, 1, 0, &c)) return st;
+  cudaError_t e = cudaMemcpyAsync((char *)c->d.state + offsetof(RunState, interval), &draw, sizeof(int),
+                                  cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) {
+    FieldArgs fa{c->d.runs, c->nruns, c->d.state, c->d_spec, c->d_tw, c->d_ybuf, c->d_maps};
+    e = launch_fields(fa, c->total_clones, c->field_max_w, c->field_max_m1, c->field_max_m2,
+                      c->field_max_tiles2, c->stream);
+  }
+  int st = clbm_status_from_cuda(e);
+  if (st == CLBM_OK) st = clbm_get_field_map(c, 0, 0, map, negative);
+  clbm_destroy(c);
+  return st;
 }

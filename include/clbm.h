@@ -166,6 +166,20 @@ int clbm_ref_perturbed_state_noalloc(double *fin, const double *snaps,
                                      double eps, int nsnap, int n,
                                      const double *prefactors, void *stream);
 
+/* generate_random_field (src/perturbation_routines/generate_random_field.cpp:9-181):
+ * one Gaussian random field with covariance exp(-r^2 / (2 sigma^2)) on a
+ * dx x dy lattice by circulant embedding, written to the HOST array map in
+ * the reference's order y + dy*x (dx*dy values).  The reference draws its
+ * normals from rand() (randNormal.cpp:4-22) and takes dx = dy; here any dx,
+ * dy <= 1024 (dy >= 4), and the normals come from a counter-based stream:
+ * (seed, draw) selects the field, and it equals the field the sampler draws
+ * for clone 0 of run 0 in interval `draw` of a context with the same seed and
+ * lattice.  Parity with the reference is statistical (same covariance).
+ * *negative (nullable) = eigenvalues of the embedding below -1e-15 (clamped
+ * to 0, the reference's `error`). */
+int clbm_ref_random_field(int dx, int dy, double sigma, unsigned long long seed,
+                          int draw, double *map, int *negative);
+
 /* ---- sampler level ------------------------------------------------------- */
 
 /* max_steps bounds the steps of one interval (drag-term storage). */

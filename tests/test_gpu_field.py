@@ -105,3 +105,30 @@ def test_forcing_driver_outputs(gpu, clbm_lib, orc, tmp_path):
             F = np.fromfile(out / f"clone_{j}" / f"evolution_{t}_clone_{j}")
             assert F.size == steps
             np.testing.assert_allclose(w[j], math.exp(alpha * (F.sum() * (1.0 / T0))), rtol=1e-12)
+
+
+def test_function_level_random_field(gpu, clbm_lib, orc):
+    """clbm_ref_random_field (generate_random_field's drop-in): the field of
+    draw t is the sampler's clone-0 field of interval t (same seed and
+    lattice), and over many draws it has the embedding's covariance."""
+    W, H, sig, seed = 40, 24, 3.0, 11
+    g = orc.channel_geom(W, H, 4, 10, 12)
+    d = run_desc(clbm_lib, g, 1, tau=0.6, beta=1e-6, field_mode=1, field_steps=1, field_eps=0.1,
+                 field_sigma=sig, seed=seed, force_scale=1.0, dt=1.0)
+    with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=2) as s:
+        s.init_equilibrium(0, 0.02, 1e-3, 1)
+        for t in range(2):
+            s.run_interval(2)
+            m, neg = clbm_lib.ref_random_field(W, H, sig, seed, t)
+            assert np.array_equal(m, s.field_map(0, 0)[0])
+            assert neg == s.field_map(0, 0)[1]
+            s.clone_step()
+    f = np.stack([clbm_lib.ref_random_field(W, H, sig, 5, t)[0].reshape(W, H) for t in range(200)])
+    lam, M1, M2 = embedding_spectrum(W, H, sig)
+    lam = np.maximum(lam, 0.0)
+    for dx, dy in [(0, 0), (1, 0), (0, 1), (3, 0), (2, 2)]:
+        expect = np.sum(lam * np.cos(2 * np.pi * (np.arange(M1)[:, None] * dx / M1 + np.arange(M2)[None, :] * dy / M2)))
+        emp = np.mean(f[:, : W - dx, : H - dy] * f[:, dx:, dy:])
+        assert abs(emp - expect) < 0.1 * max(expect, 0.2), (dx, dy, emp, expect)
+    with pytest.raises(clbm_lib.ClbmError):
+        clbm_lib.ref_random_field(2000, 24, sig, 1, 0)
