@@ -70,7 +70,16 @@ __device__ __forceinline__ void drag_grad(const RunDev &R, int x, int y, const T
   }
 }
 
-// sigma_S = J_C(S)^T pi for the BGK + Guo collision of clbm_physics.cuh
+// sigma_S = J_C(S)^T pi for the BGK + Guo collision of clbm_physics.cuh.
+// The collision is (1 - omega) I plus a function of rho, ux, uy, so
+// J^T pi = (1 - omega) pi + A + c_k (Bx, By) with G = d/d(rho, ux, uy) of
+// sum_k pi_k (omega feq_k + F_k).  Written through the weighted moments of pi
+// (P0 = sum w pi, Px = sum w cx pi, ..., Pxy = sum w cx cy pi), the sums over
+// k of the per-k derivatives collapse to a few products:
+//   G0 = omega (P0 (1 - u2) + 3 (ux Px + uy Py) + 4.5 (ux^2 Pxx + 2 ux uy Pxy + uy^2 Pyy))
+//   Gx = omega rho (3 Px + 9 (ux Pxx + uy Pxy) - 3 ux P0) + cf beta (9 Pxx - 3 P0)
+//   Gy = omega rho (3 Py + 9 (ux Pxy + uy Pyy) - 3 uy P0) + 9 cf beta Pxy
+// (u2 = 1.5 |u|^2, cf the Guo prefactor, feq and F as in collide_ref64).
 template <typename T>
 __device__ __forceinline__ void collide_adjoint(const RunDev &R, const T S[9], const T pi[9],
                                                 T out[9]) {
@@ -82,22 +91,23 @@ __device__ __forceinline__ void collide_adjoint(const RunDev &R, const T S[9], c
   const T jy = (S[2] - S[4]) + ((S[5] - S[7]) + (S[6] - S[8]));
   const T ux = (jx + T(0.5) * beta) / rho, uy = jy / rho;
   const T u2 = T(1.5) * (ux * ux + uy * uy);
-  T G0 = 0, Gx = 0, Gy = 0;
-#pragma unroll
-  for (int k = 0; k < 9; k++) {
-    const T cx = (T)cx_of(k), cy = (T)cy_of(k), w = (T)w_of(k);
-    const T e = cx * ux + cy * uy;
-    const T dfeq_drho = w * (T(1) + T(3) * e + T(4.5) * e * e - u2);
-    const T dG_dux = omega * w * rho * (T(3) * cx + T(9) * e * cx - T(3) * ux) +
-                     w * cf * beta * (T(-3) + T(9) * cx * cx);
-    const T dG_duy = omega * w * rho * (T(3) * cy + T(9) * e * cy - T(3) * uy) +
-                     w * cf * beta * (T(9) * cx * cy);
-    G0 += pi[k] * omega * dfeq_drho;
-    Gx += pi[k] * dG_dux;
-    Gy += pi[k] * dG_duy;
-  }
-  const T A = G0 - (ux * Gx + uy * Gy) / rho;
-  const T Bx = Gx / rho, By = Gy / rho;
+  const T wa = T(1) / T(9), wd = T(1) / T(36);
+  const T a13 = pi[1] + pi[3], a24 = pi[2] + pi[4];
+  const T dsum = (pi[5] + pi[7]) + (pi[6] + pi[8]);
+  const T P0 = T(4) / T(9) * pi[0] + wa * (a13 + a24) + wd * dsum;
+  const T Px = wa * (pi[1] - pi[3]) + wd * ((pi[5] - pi[7]) + (pi[8] - pi[6]));
+  const T Py = wa * (pi[2] - pi[4]) + wd * ((pi[5] - pi[7]) + (pi[6] - pi[8]));
+  const T Pxx = wa * a13 + wd * dsum;
+  const T Pyy = wa * a24 + wd * dsum;
+  const T Pxy = wd * ((pi[5] + pi[7]) - (pi[6] + pi[8]));
+  const T G0 = omega * (P0 * (T(1) - u2) + T(3) * (ux * Px + uy * Py) +
+                        T(4.5) * (ux * ux * Pxx + T(2) * ux * uy * Pxy + uy * uy * Pyy));
+  const T Gx = omega * rho * (T(3) * Px + T(9) * (ux * Pxx + uy * Pxy) - T(3) * ux * P0) +
+               cf * beta * (T(9) * Pxx - T(3) * P0);
+  const T Gy = omega * rho * (T(3) * Py + T(9) * (ux * Pxy + uy * Pyy) - T(3) * uy * P0) + T(9) * cf * beta * Pxy;
+  const T inv = T(1) / rho;
+  const T A = G0 - (ux * Gx + uy * Gy) * inv;
+  const T Bx = Gx * inv, By = Gy * inv;
 #pragma unroll
   for (int k = 0; k < 9; k++) out[k] = om1 * pi[k] + A + (T)cx_of(k) * Bx + (T)cy_of(k) * By;
 }
@@ -114,7 +124,7 @@ __global__ void __launch_bounds__(STEP_BLOCK) k_adj_step(AdjArgs a) {
   const T *sig = (const T *)a.sigma_in + cb;
   const T *P = (const T *)a.P + cb;
   T *out = (T *)a.sigma_out + cb;
-  const int W = R.W, y = n / W, x = n - y * W;
+  const int W = R.W, y = (int)__umulhi((unsigned)n, R.div_w), x = n - y * W;
   const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
   const int mask = (in_box || y == 0 || y == R.H - 1) ? bounce_mask(R, x, y) : 0;
   if (mask & 512) {
@@ -170,7 +180,7 @@ __global__ void __launch_bounds__(STEP_BLOCK) k_adj_init(AdjArgs a) {
   const long long cb = R.pop_base + (long long)clone * 9 * plane;
   const T *P = (const T *)a.P + cb;
   T *out = (T *)a.sigma_out + cb;
-  const int W = R.W, y = n / W, x = n - y * W;
+  const int W = R.W, y = (int)__umulhi((unsigned)n, R.div_w), x = n - y * W;
   const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
   const int mask = in_box ? bounce_mask(R, x, y) : 0;
   if (!in_box || (mask & 512)) {
