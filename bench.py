@@ -372,8 +372,9 @@ def main():
     # the streaming step kernel's own roofline, from the autotuner's timing of
     # its best launch variant on this workload (one launch per step)
     stream_ref = None
-    if len(tune_ms) >= clbm.STREAM_VARIANTS:
-        sms = min(float(x) for x in tune_ms[:clbm.STREAM_VARIANTS] if x > 0)
+    stream_ms = [float(x) for x in tune_ms[:clbm.STREAM_VARIANTS] if x > 0]
+    if cluster and stream_ms:
+        sms = min(stream_ms)
         sa = bpl * nodes_total / (sms / 1e3) / 1e9
         stream_ref = {"kernel": "k_step_f32", "ms_per_step": sms, "achieved": sa, "frac": sa / peak,
                       "traffic": ncu_traffic(f"k_step_f32_{args.workload}.md")}
