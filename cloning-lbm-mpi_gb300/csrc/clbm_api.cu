@@ -895,7 +895,7 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
       if (ms_per_variant) ms_per_variant[vidx] = -1.0;
       bool ok = true;
       for (const RunDev &R : c->runs_h)
-        if (R.H % cs || temporal_max_clusters(cs, tv, R.W, R.H, R.field_mode != 0) < 1) ok = false;
+        if (R.H < cs || temporal_max_clusters(cs, tv, R.W, R.H, R.field_mode != 0) < 1) ok = false;
       if (!ok) continue;
       cudaError_t e = cudaEventRecord(e0, c->stream);
       for (int r = 0; r < c->nruns && e == cudaSuccess; r++) {
@@ -945,7 +945,7 @@ extern "C" int clbm_set_step_variant(clbm_ctx *c, int variant) {
     const int q = variant - step_variant_count();
     const int cs = 1 << (q / temporal_variant_count()), tv = q % temporal_variant_count();
     for (const RunDev &R : c->runs_h)
-      if (R.H % cs || temporal_max_clusters(cs, tv, R.W, R.H, R.field_mode != 0) < 1)
+      if (R.H < cs || temporal_max_clusters(cs, tv, R.W, R.H, R.field_mode != 0) < 1)
         return fail(CLBM_ERR_INVALID, "cluster shape does not fit this workload");
   }
   apply_variant(c, variant);

@@ -1,9 +1,10 @@
 // clbm_temporal.cu -- FP32 interval kernel with every clone resident on chip.
 //
 // One thread-block cluster per clone: the clone's H rows are split into CS
-// bands of R = H/CS rows, each band in one CTA's shared memory (9 planes of
-// R*W floats).  The T steps of the interval run without touching HBM except
-// for the drag terms: P_0 is loaded once, S_T stored once.
+// bands of H/CS rows (the first H % CS bands one more), each band in one
+// CTA's shared memory (nine floats per node, node after node).  The T steps
+// of the interval run without touching HBM except for the drag terms: P_0 is
+// loaded once, S_T stored once.
 //
 // In-place update ("AA" pattern): one buffer A holds, alternately,
 //   after a local step:  A[n][opp k] = P(n,k)        (post-collision, own node)
@@ -48,6 +49,7 @@ __device__ __forceinline__ void st_cluster(unsigned a, float v) {
 // Geometry of one CTA's band.
 struct Band {
   int cs, rank, clone, W, H, rows, row0, nb, rowstep;
+  int rows_prev;  // rows of the previous band (its last row lies above this band's row 0)
   float *prev, *next;
   unsigned own_c, prev_c, next_c;  // shared::cluster byte addresses of A in this / previous / next CTA
   long long plane;
@@ -85,7 +87,7 @@ __device__ __forceinline__ void update_general(const TemporalArgs &a, const Band
       const int sxc = cx == 1 ? cm : (cx == -1 ? cp : c0);  // column, row ly
       const int sl = ly - cy;                                 // source row, band-local
       const float *base = sl < 0 ? b.prev : (sl >= rows ? b.next : A);
-      const int roff = sl < 0 ? (rows - 1 - ly) * rowstep : (sl >= rows ? -ly * rowstep : -cy * rowstep);
+      const int roff = sl < 0 ? (b.rows_prev - 1 - ly) * rowstep : (sl >= rows ? -ly * rowstep : -cy * rowstep);
       S[k] = base[sxc + roff + opp_of(k)];
     }
   }
@@ -120,7 +122,7 @@ __device__ __forceinline__ void update_general(const TemporalArgs &a, const Band
       const int txc = cx == 1 ? cp : (cx == -1 ? cm : c0);
       const int tl = ly + cy;
       float *base = tl < 0 ? b.prev : (tl >= rows ? b.next : A);
-      const int roff = tl < 0 ? (rows - 1 - ly) * rowstep : (tl >= rows ? -ly * rowstep : cy * rowstep);
+      const int roff = tl < 0 ? (b.rows_prev - 1 - ly) * rowstep : (tl >= rows ? -ly * rowstep : cy * rowstep);
       base[txc + roff + k] = P[k];
     }
   }
@@ -144,7 +146,7 @@ __device__ __forceinline__ void update_general_gather(const TemporalArgs &a, con
   if (mask & 512) return;  // inside the square
   // byte addresses of column 0 of the rows y-1, y, y+1
   const unsigned rowC = b.own_c + 4u * (unsigned)(ly * rs);
-  const unsigned rowU = ly == 0 ? b.prev_c + 4u * (unsigned)((rows - 1) * rs) : rowC - 4u * (unsigned)rs;
+  const unsigned rowU = ly == 0 ? b.prev_c + 4u * (unsigned)((b.rows_prev - 1) * rs) : rowC - 4u * (unsigned)rs;
   const unsigned rowD = ly == rows - 1 ? b.next_c : rowC + 4u * (unsigned)rs;
   const unsigned own = rowC + 36u * (unsigned)x;
   unsigned ad[9];
@@ -215,8 +217,11 @@ __device__ __forceinline__ Band make_band(const TemporalArgs &a, float *A, cg::c
   b.clone = blockIdx.x / b.cs;
   b.W = a.rd.W;
   b.H = a.rd.H;
-  b.rows = b.H / b.cs;
-  b.row0 = b.rank * b.rows;
+  // H rows over cs bands: the first H % cs bands take one row more
+  const int base = b.H / b.cs, extra = b.H % b.cs;
+  b.rows = base + (b.rank < extra ? 1 : 0);
+  b.row0 = b.rank * base + min(b.rank, extra);
+  b.rows_prev = b.rank > 0 ? base + (b.rank - 1 < extra ? 1 : 0) : b.rows;
   b.nb = b.rows * b.W;
   b.rowstep = b.W * 9;
   b.prev = b.rank > 0 ? cluster.map_shared_rank(A, b.rank - 1) : A;
@@ -397,6 +402,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
 
 typedef void (*TemporalFn)(TemporalArgs);
 
+// rows of the largest band (the first H % cs bands take one row more)
+static int band_rows_max(int H, int cs) { return (H + cs - 1) / cs; }
+
 struct TemporalVariant {
   int threads;
   TemporalFn fn[2];  // [field]
@@ -410,8 +418,8 @@ int temporal_variant_count() { return (int)(sizeof(kTemporal) / sizeof(kTemporal
 
 // the kernel of a variant for this band shape, or nullptr when it cannot run it
 static TemporalFn temporal_fn(int variant, int cs, int W, int H, bool field) {
-  if (variant < 0 || variant >= temporal_variant_count() || cs < 1 || H % cs) return nullptr;
-  if (temporal_smem((H / cs) * W) > 227 * 1024) return nullptr;
+  if (variant < 0 || variant >= temporal_variant_count() || cs < 1 || H < cs) return nullptr;
+  if (temporal_smem(band_rows_max(H, cs) * W) > 227 * 1024) return nullptr;
   return kTemporal[variant].fn[field];
 }
 
@@ -437,13 +445,13 @@ static cudaError_t prepare(TemporalFn fn, int cs, size_t smem) {
   return e;
 }
 
-// Launch one run's interval with cluster size cs (H % cs == 0).
+// Launch one run's interval with cluster size cs (cs <= H).
 cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W, int H,
                             cudaStream_t s) {
   const bool field = a.rd.field_mode != 0 && a.maps != nullptr;
   TemporalFn fn = temporal_fn(variant, cs, W, H, field);
   if (!fn || a.steps < 1) return cudaErrorInvalidConfiguration;
-  const size_t smem = temporal_smem((H / cs) * W);
+  const size_t smem = temporal_smem(band_rows_max(H, cs) * W);
   cudaError_t e = prepare(fn, cs, smem);
   if (e != cudaSuccess) return e;
   cudaLaunchAttribute attr[1];
@@ -455,7 +463,7 @@ cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclo
 int temporal_max_clusters(int cs, int variant, int W, int H, bool field) {
   TemporalFn fn = temporal_fn(variant, cs, W, H, field);
   if (!fn) return 0;
-  const size_t smem = temporal_smem((H / cs) * W);
+  const size_t smem = temporal_smem(band_rows_max(H, cs) * W);
   if (prepare(fn, cs, smem) != cudaSuccess) return 0;
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = temporal_config(cs, variant, 64, smem, nullptr, attr);

@@ -1,9 +1,10 @@
 """The cluster-resident FP32 interval kernel (every clone in the shared
 memory of one thread-block cluster for a whole interval) must give results
 bit-identical to the streaming step kernel: same pull rules, same collision
-arithmetic.  Cases cover cluster sizes 1, 2 and 4 with the square across
-band edges, a width that is not a multiple of 32, copies and perturbations
-between intervals, and the random body-force field."""
+arithmetic.  Cases cover cluster sizes 1, 2, 4 and 8 with the square across
+band edges, heights that the cluster size does not divide (uneven bands), a
+width that is not a multiple of 32, copies and perturbations between
+intervals, and the random body-force field."""
 import numpy as np
 import pytest
 
@@ -28,6 +29,9 @@ def temporal_variant(cs, tv=0):
     (64, 24, 6, 16, 12, 4, 2, False),
     (200, 32, 8, 50, 16, 4, 0, True),
     (96, 16, 5, 30, 9, 2, 2, True),
+    (64, 25, 6, 16, 12, 4, 0, False),    # H % cs != 0: bands of 7, 6, 6, 6 rows
+    (96, 23, 5, 30, 9, 4, 2, True),      # bands of 6, 6, 6, 5 rows, field
+    (200, 50, 8, 50, 25, 8, 1, False),   # bands of 7 and 6 rows, square across bands
 ])
 def test_temporal_equals_streaming(gpu, clbm_lib, orc, W, H, side, xc, yc, cs, tv, field):
     g = orc.channel_geom(W, H, side, xc, yc)
