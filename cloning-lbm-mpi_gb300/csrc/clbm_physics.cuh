@@ -173,7 +173,10 @@ __device__ __forceinline__ float collide_f32_pairs(const float g[9], float out[9
   const float jx = add(sub(g[1], g[3]), add(s57, sub(g[8], g[6])));
   const float jy = add(sub(g[2], g[4]), add(s57, sub(g[6], g[8])));
   const float rho = add(1.0f, drho);
-  const float inv = __frcp_rn(rho);
+  // 1/rho: the hardware approximation refined by one Newton-Raphson step,
+  // r1 = r0 + r0 (1 - rho r0) (rho is near 1: no special operands)
+  const float r0 = __fdividef(1.0f, rho);
+  const float inv = fma(r0, fma(-rho, r0, 1.0f), r0);
   const float ux = mul(fma(0.5f, beta, jx), inv);
   const float uy = mul(jy, inv);
   const float u2 = mul(1.5f, fma(ux, ux, mul(uy, uy)));
