@@ -103,3 +103,34 @@ def test_graph_replay_with_cluster_resident_kernel(gpu, clbm_lib, orc):
         assert np.array_equal(np.concatenate(rv, axis=1), ref)
         for j in range(nc):
             assert np.array_equal(s.dump(0, j), ref_state[j])
+
+
+def test_bench_lattice_at_bench_shape(gpu, clbm_lib, orc):
+    """The bench's clone lattice (256x64, square 12) at the bench's interval
+    length and the shape the autotuner picks there (cluster size 4, 1024
+    threads): bit-identical to the streaming kernel, and mass conserved
+    (bounce-back and the body force keep sum f; FP32 rounding only)."""
+    from clbm import configs
+    r = configs.WORKLOADS["c3"]().runs[0]
+    g = orc.channel_geom(r.width, r.height, r.side, r.xc, r.yc)
+    d = clbm_lib.RunDesc(width=g.nx, height=g.ny, xmin=g.xmin, xmax=g.xmax, ymin=g.ymin, ymax=g.ymax,
+                         nclones=8, ranks=1, tau=r.tau, beta=r.beta, alpha=r.k, force_scale=1.0 / r.F0,
+                         dt=r.dt, perturb_mode=clbm_lib.PERTURB_UNIFORM, eps=1e-3, seed=5)
+    T = 100
+    out = []
+    for variant in (7, temporal_variant(4, 0)):
+        with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T) as s:
+            s.set_step_variant(variant)
+            s.init_equilibrium(0, r.u0, 1e-3, 9)
+            m0 = [s.dump(0, j).sum() for j in range(8)]
+            s.run_interval(T)
+            res = [s.drag(0)] + [s.dump(0, j) for j in range(8)]
+            for j in range(8):
+                assert abs(res[1 + j].sum() - m0[j]) < 1e-6 * m0[j]
+            s.clone_step()
+            s.run_interval(T)
+            res += [s.drag(0)] + [s.dump(0, j) for j in range(8)]
+            assert s.error_word() == 0
+            out.append(res)
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
