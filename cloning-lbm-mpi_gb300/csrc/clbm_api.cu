@@ -864,7 +864,7 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
   for (int v = 0; v < nv; v++) {
     StepArgs a{c->d.runs, c->nruns, 0, c->pop[c->s_buf], c->pop[1 - c->s_buf], c->d.terms,
                c->d.term_slab, c->d.err, c->total_clones, c->max_nodes,
-               {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}};
+               {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}, c->d_maps};
     cudaError_t e = launch_step(false, false, a, c->total_blocks, c->stream, v);  // warm-up
     if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
     for (int i = 0; i < launches && e == cudaSuccess; i++)
@@ -1003,6 +1003,8 @@ extern "C" int clbm_drag_fwd(clbm_ctx *c, int steps, int every, double *J) {
   if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
   if (steps < 1 || steps > c->max_steps || every < 1) return fail(CLBM_ERR_INVALID, "bad steps / checkpoint period");
   if (c->pending) return fail(CLBM_ERR_INVALID, "a clone step is pending; run an interval first");
+  if (c->any_field)
+    return fail(CLBM_ERR_INVALID, "the adjoint covers the constant body force only (a run has a random field)");
   const bool f64 = c->precision == CLBM_FP64;
   const size_t pop = c->pop_elems * c->elem_size;
   const size_t nckpt = (size_t)(steps + every - 1) / every;
@@ -1021,12 +1023,13 @@ extern "C" int clbm_drag_fwd(clbm_ctx *c, int steps, int every, double *J) {
     return (t % every == 0) ? c->adj.ckpt + (size_t)(t / every) * pop : c->adj.sig[t % 2];
   };
   ReseedArgs ra{c->d.runs, c->nruns, c->adj.s0, loc(0), c->d_identity, c->d_zeros, c->d.pert,
-                c->d.prefactors, c->d.snaps, c->d.state, c->d.err};
+                c->d.prefactors, c->d.snaps, c->d.state, c->d.err, nullptr};
   CK(launch_reseed(f64, ra, c->total_blocks, s));
   for (int t = 0; t < steps; t++) {
     char *dst = (t + 1 < steps) ? loc(t + 1) : c->adj.sig[(t + 1) % 2];
     StepArgs a{c->d.runs, c->nruns, t, loc(t), dst, c->d.terms, c->d.term_slab, c->d.err,
-               c->total_clones, c->max_nodes, {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}};
+               c->total_clones, c->max_nodes, {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]},
+               nullptr};
     CK(launch_step(f64, false, a, c->total_blocks, s, c->step_variant));
   }
   CK(launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, s));
@@ -1056,7 +1059,7 @@ extern "C" int clbm_drag_bwd(clbm_ctx *c) {
     for (int p = lo; p < hi; p++) {  // recompute P_lo .. P_hi from the checkpoint
       StepArgs a{c->d.runs, c->nruns, 0, segP(lo, p), segP(lo, p + 1), c->d.terms, c->d.term_slab,
                  c->d.err, c->total_clones, c->max_nodes,
-                 {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}};
+                 {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}, nullptr};
       CK(launch_step(f64, false, a, c->total_blocks, s, c->step_variant));
     }
     for (int p = hi; p >= lo; p--) {

@@ -56,3 +56,13 @@ def test_adjoint_vs_central_differences(gpu, clbm_lib, orc, prec, tol):
             ad = (grad * dirn).reshape(nc, n).sum(axis=1)
             err = np.abs(ad - fd) / np.abs(fd)
             assert (err < tol).all(), (err, ad, fd)
+
+
+def test_adjoint_rejects_random_field_runs(gpu, clbm_lib, orc):
+    g, phys, d = case(orc, clbm_lib)
+    d.field_mode, d.field_steps, d.field_eps, d.field_sigma = 1, 5, 0.2, 4.0
+    with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=10) as s:
+        s.init_equilibrium(0, 0.05, 1e-3, 1)
+        with pytest.raises(clbm_lib.ClbmError) as e:
+            s.drag_fwd(10, 5)
+        assert e.value.status == clbm_lib.ERR_INVALID
