@@ -130,3 +130,21 @@ def test_bodyforce_warmup_and_snapshots(drivers, orc, tmp_path):
     assert np.array_equal(np.fromfile(tmp_path / "run" / "ux_t.datout"), np.array(ux))
     assert len(list((tmp_path / "run" / "vtk_fluid").glob("fluid_t*.vtk"))) == 3
     assert (tmp_path / "run" / "popfiles_list.dat").read_text().split() == [f"pops_{k}.datout" for k in range(3)]
+
+
+def test_pops_driver_fp32_first_interval(drivers, orc, tmp_path):
+    """--fp32 (the driver autotunes the interval kernel): the first interval's
+    force series of every clone within 1e-5 of the reference driver's (the
+    genealogy may differ later, FP32 rounding can flip a resampling draw)."""
+    z = np.load(GOLD / "pops_driver.npz")
+    L, Nc, U0, tau, alpha, eps, T, dT = z["params"][0]
+    p = dict(L=int(L), Nc=int(Nc), U0=U0, tau=tau, alpha=alpha, eps=eps, T=T, dT=dT)
+    stage_pops_run(orc, tmp_path, p)
+    r = subprocess.run([str(drivers / "TLGK_LBM_POPS_PERTURB"), "--fp32", "input"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    steps = orc.reference_scalars(int(L), U0, dT, T)["steps"]
+    for j in range(int(Nc)):
+        f = np.fromfile(tmp_path / "out" / f"clone_{j}" / "data_force.datout")[:steps]
+        g = z["run0_force"][j][:steps]
+        assert np.abs(f - g).max() <= 1e-5 * np.abs(g).max()
