@@ -4,6 +4,7 @@ import ctypes as C
 import re
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 REPO = Path(__file__).resolve().parent.parent
@@ -41,6 +42,10 @@ def test_invalid_arguments_are_rejected(clbm_lib):
     assert L.clbm_create(C.byref(ok), 1, 0, 10, 0, C.byref(h)) == clbm_lib.ERR_INVALID  # ranks
     g = clbm_lib.Geom(2, 2, 0, 0, 0, 0)
     assert L.clbm_ref_walls_bb(C.byref(g), None, None, None) == clbm_lib.ERR_INVALID
+    m = np.zeros(16)
+    assert L.clbm_ref_random_field(2, 8, 3.0, 1, 0, m.ctypes.data_as(C.c_void_p), None) == clbm_lib.ERR_INVALID
+    assert L.clbm_ref_random_field(8, 8, -1.0, 1, 0, m.ctypes.data_as(C.c_void_p), None) == clbm_lib.ERR_INVALID
+    assert L.clbm_ref_random_field(8, 8, 3.0, 1, 0, None, None) == clbm_lib.ERR_INVALID
 
 
 def test_no_device_means_status_not_fallback(clbm_lib):
