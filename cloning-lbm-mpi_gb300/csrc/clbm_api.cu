@@ -126,6 +126,25 @@ static bool geometry_ok(const clbm_run_desc &r) {
   return true;
 }
 
+// FP32 collision constants with exactly consistent relaxation factors:
+// c2 = omega/12 rounded to a multiple of 2^-25, c13 = (omega - 4 c2)/2
+// rounded to a multiple of 2^-24, omega' = 2 c13 + 4 c2 (a multiple of 2^-23,
+// within 3e-8 of omega), om1 = 1 - omega' and cforce = 1 - omega'/2; every
+// one of them is exactly representable in FP32, which is checked.
+static bool f32_collision_constants(double omega, RunDev &R) {
+  const double c2 = std::nearbyint(omega / 12.0 * 33554432.0) / 33554432.0;
+  const double c13 = std::nearbyint((omega - 4.0 * c2) / 2.0 * 16777216.0) / 16777216.0;
+  const double om = 2.0 * c13 + 4.0 * c2;
+  if (!(c2 > 0.0 && c13 > 0.0 && om > 0.0 && om <= 2.0)) return false;
+  R.f_omega = (float)om;
+  R.f_om1 = (float)(1.0 - om);
+  R.f_c13 = (float)c13;
+  R.f_c2 = (float)c2;
+  R.f_cforce = (float)(1.0 - 0.5 * om);
+  return (double)R.f_omega == om && (double)R.f_om1 == 1.0 - om && (double)R.f_c13 == c13 &&
+         (double)R.f_c2 == c2 && (double)R.f_cforce == 1.0 - 0.5 * om;
+}
+
 static void destroy_graphs(clbm_ctx *c) {
   for (auto &g : c->graphs) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
@@ -243,9 +262,12 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
     R.force_shift = d.force_shift;
     R.dt = d.dt;
     R.eps = d.eps;
-    R.f_omega = (float)R.omega;
-    R.f_cforce = (float)R.cforce;
+    if (!f32_collision_constants(R.omega, R)) {
+      delete c;
+      return fail(CLBM_ERR_INVALID, "tau out of range for the FP32 collision (need 0.5 < tau)");
+    }
     R.f_beta = (float)d.beta;
+    R.f_force = f32_force(R.f_beta, R.f_cforce);
     R.perturb_mode = d.perturb_mode;
     R.resample_mode = d.resample_mode;
     R.ranks = d.ranks < 1 ? 1 : d.ranks;

@@ -34,6 +34,31 @@ enum : unsigned {
   ERR_TIMEOUT = 1u << 5,
 };
 
+// Body-force terms of the FP32 collision for one value of beta:
+// hb = beta/2 (velocity shift), fb = cforce beta, fbm3 = -3 fb, fb9 = 9 fb,
+// f13 = fb/3 and f2 = fb/12 (the odd Guo terms of the axis and diagonal
+// pairs).  Plain IEEE single-precision products, so the host (uniform runs)
+// and the device (a random field, per node) get the same bits for one beta.
+struct F32Force {
+  float hb, fb, fbm3, fb9, f13, f2;
+};
+__host__ __device__ inline F32Force f32_force(float beta, float cforce) {
+#ifdef __CUDA_ARCH__
+#define CLBM_FMUL __fmul_rn
+#else
+#define CLBM_FMUL(a, b) ((float)(a) * (float)(b))
+#endif
+  F32Force f;
+  f.hb = CLBM_FMUL(0.5f, beta);
+  f.fb = CLBM_FMUL(cforce, beta);
+  f.fbm3 = CLBM_FMUL(-3.0f, f.fb);
+  f.fb9 = CLBM_FMUL(9.0f, f.fb);
+  f.f13 = CLBM_FMUL(f.fb, 1.0f / 3.0f);
+  f.f2 = CLBM_FMUL(f.fb, 1.0f / 12.0f);
+#undef CLBM_FMUL
+  return f;
+}
+
 // One independent run (lattice, square, physics, clone block) of a batch.
 struct RunDev {
   int W, H;                    // Dx, Dy
@@ -59,7 +84,11 @@ struct RunDev {
   double tau, omega, om1, cforce, beta;
   double wcb[9];               // (w[k]*cforce)*beta, the reference's order
   double alpha, force_scale, force_shift, dt, eps;
-  float f_omega, f_cforce, f_beta, f_pad;
+  // FP32 collision: omega' = 2 c13 + 4 c2 exactly (c13 ~ omega/3 on a 2^-24
+  // grid, c2 ~ omega/12 on a 2^-25 grid), om1 = 1 - omega' and
+  // cforce = 1 - omega'/2 exactly; f_force = f32_force(f_beta, f_cforce)
+  float f_omega, f_om1, f_c13, f_c2, f_cforce, f_beta;
+  F32Force f_force;
   int perturb_mode, resample_mode, ranks, nsnap;
   unsigned long long seed;
   unsigned run_id;

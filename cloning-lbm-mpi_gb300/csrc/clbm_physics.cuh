@@ -113,34 +113,7 @@ __device__ __forceinline__ void pi_ref64(const double f[9], double &rho, double 
 // ------------------------------------------------------------------ f32 ----
 // Shifted populations g = f - w.  With drho = rho - 1:
 //   geq_k = feq_k - w_k = w_k (drho + rho (3 eu + 4.5 eu^2 - 1.5 u^2))
-//   g*_k  = g_k + omega (geq_k - g_k) + F_k
-__device__ __forceinline__ void collide_f32(const float g[9], float out[9], float beta,
-                                            float omega, float cforce, float *rho_o = nullptr,
-                                            float *ux_o = nullptr, float *uy_o = nullptr) {
-  const float drho = ((g[0] + (g[1] + g[3])) + (g[2] + g[4])) + ((g[5] + g[7]) + (g[6] + g[8]));
-  const float jx = (g[1] - g[3]) + ((g[5] - g[7]) + (g[8] - g[6]));
-  const float jy = (g[2] - g[4]) + ((g[5] - g[7]) + (g[6] - g[8]));
-  const float rho = 1.0f + drho;
-  const float inv = 1.0f / rho;
-  const float ux = (jx + 0.5f * beta) * inv;
-  const float uy = jy * inv;
-  const float u2 = 1.5f * (ux * ux + uy * uy);
-  const float fb = cforce * beta;
-#pragma unroll
-  for (int k = 0; k < 9; k++) {
-    const int cx = cx_of(k), cy = cy_of(k);
-    const float eu = (float)cx * ux + (float)cy * uy;
-    const float wk = (float)w_of(k);
-    const float geq = wk * (drho + rho * (eu * (3.0f + 4.5f * eu) - u2));
-    const float drive = wk * fb * (3.0f * ((float)cx - ux) + 9.0f * (float)cx * eu);
-    out[k] = g[k] + omega * (geq - g[k]) + drive;
-  }
-  if (rho_o) {
-    *rho_o = rho;
-    *ux_o = ux;
-    *uy_o = uy;
-  }
-}
+//   g*_k  = (1 - omega) g_k + omega geq_k + F_k
 
 // FP32 body force of a node under a random field: beta (1 + eps m), with
 // explicit rounding steps so that no kernel contracts or reorders it
@@ -150,13 +123,6 @@ __device__ __forceinline__ float field_beta_f32(float beta, float eps, float m) 
   return __fmul_rn(beta, __fmaf_rn(eps, m, 1.0f));
 }
 
-// The same collision organised by opposite pairs (k, opp k): they share
-// |c.u|, so with e = c_k.u the equilibria split into an even part
-// w (drho + rho (4.5 e^2 - 1.5 u^2)) and an odd part +-3 w rho e, and the
-// Guo terms into w fb (9 cx e - 3 ux) and +-3 w fb cx.  Returns drho.
-// Every operation is an explicitly rounded intrinsic (the fused multiply-adds
-// chosen here, none left to the compiler), so the result is the same bit for
-// bit in every kernel that inlines it, whatever it knows about beta.
 namespace f32op {
 __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
@@ -164,8 +130,36 @@ __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b);
 __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 }  // namespace f32op
 
-__device__ __forceinline__ float collide_f32_pairs(const float g[9], float out[9], float beta,
-                                                   float omega, float cforce) {
+// The collision organised by opposite pairs (k, opp k): they share |c.u|, so
+// with e = c_k.u the equilibria split into an even part
+// w (drho + rho (4.5 e^2 - 1.5 u^2)) and an odd part +-3 w rho e, and the
+// Guo terms into w fb (9 cx e - 3 ux) and +-3 w fb cx.  Returns drho.
+//
+// Free of systematic rounding bias in the momentum.  The equilibrium
+// momentum rho u (~0.05) is ~10^4 times the body force added per step
+// (~1e-6), so a rounding that errs the same way at every node and step,
+// even by a fraction of an ulp, acts as a spurious body force of a sizeable
+// fraction of the real one and the flow drifts over an interval series.
+// Three such roundings are avoided:
+//  * the velocity shift: jx + beta/2 rounds a fixed offset onto the grid of
+//    jx, the same error at every node; ux = jx/rho + (beta/2)/rho is formed
+//    by one fused multiply-add of the exact product jx * (1/rho) instead;
+//  * the weights: the odd parts carry the momentum through the coefficients
+//    3 w omega, and float(1/9) is 7.5e-9 too large, which puts 7.5e-9 rho u
+//    of momentum into every node and step; the coefficients here are
+//    c13 ~ omega/3 and c2 ~ omega/12 with omega' = 2 c13 + 4 c2 and
+//    om1 = 1 - omega' exact, so the odd parts relax the momentum by exactly
+//    the factor the (1 - omega') g_k terms leave;
+//  * rho near 1: omega * (3 rho) rounds a near-constant product the same way
+//    at many nodes; the odd parts use rho u = ux + drho ux instead, a fused
+//    multiply-add of an exact product.
+// The remaining roundings act on operands with effectively random low bits.
+// Every operation is an explicitly rounded intrinsic (the fused
+// multiply-adds chosen here, none left to the compiler), so the result is the
+// same bit for bit in every kernel that inlines it.
+__device__ __forceinline__ float collide_f32_pairs(const float g[9], float out[9], float omega,
+                                                   float om1, float c13, float c2,
+                                                   const F32Force &f) {
   using namespace f32op;
   const float a57 = add(g[5], g[7]), a68 = add(g[6], g[8]);
   const float s57 = sub(g[5], g[7]);
@@ -173,52 +167,62 @@ __device__ __forceinline__ float collide_f32_pairs(const float g[9], float out[9
   const float jx = add(sub(g[1], g[3]), add(s57, sub(g[8], g[6])));
   const float jy = add(sub(g[2], g[4]), add(s57, sub(g[6], g[8])));
   const float rho = add(1.0f, drho);
-  // 1/rho: the hardware approximation refined by one Newton-Raphson step,
-  // r1 = r0 + r0 (1 - rho r0) (rho is near 1: no special operands)
+  // 1/(1 + drho): the hardware approximation r0 of 1/rho refined by one
+  // Newton-Raphson step on the unrounded density, r0 + r0 ((1 - r0) - drho r0)
+  // (1 - r0 is exact: r0 is near 1)
   const float r0 = __fdividef(1.0f, rho);
-  const float inv = fma(r0, fma(-rho, r0, 1.0f), r0);
-  const float ux = mul(fma(0.5f, beta, jx), inv);
+  const float inv = fma(r0, fma(-drho, r0, sub(1.0f, r0)), r0);
+  const float ux = fma(jx, inv, mul(f.hb, inv));
   const float uy = mul(jy, inv);
+  const float tx = fma(drho, ux, ux), ty = fma(drho, uy, uy);  // rho u
   const float u2 = mul(1.5f, fma(ux, ux, mul(uy, uy)));
-  const float fb = mul(cforce, beta);
-  const float fb3 = mul(3.0f, fb), fb9 = mul(9.0f, fb);
-  const float om1 = sub(1.0f, omega);
   const float base = fma(-rho, u2, drho);  // even part before the e^2 term (per unit weight)
-  const float fx = mul(mul(-3.0f, fb), ux);  // Guo even part for cx = 0 (per unit weight)
+  const float fx = mul(f.fbm3, ux);         // Guo even part for cx = 0 (per unit weight)
   // k = 0
   out[0] = fma(om1, g[0], mul(4.0f / 9.0f, fma(omega, base, fx)));
-  const float r45 = mul(4.5f, rho), or3 = mul(omega, mul(3.0f, rho));
+  const float r45 = mul(4.5f, rho);
   // axis pairs (1,3): e = ux, cx = 1; (2,4): e = uy, cx = 0
   {
     const float w = 1.0f / 9.0f, e = ux;
-    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(fb9, e, fx)));
-    const float od = mul(w, fma(or3, e, fb3));
+    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(f.fb9, e, fx)));
+    const float od = fma(c13, tx, f.f13);
     out[1] = fma(om1, g[1], add(ev, od));
     out[3] = fma(om1, g[3], sub(ev, od));
   }
   {
     const float w = 1.0f / 9.0f, e = uy;
     const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fx));
-    const float od = mul(w, mul(or3, e));
+    const float od = mul(c13, ty);
     out[2] = fma(om1, g[2], add(ev, od));
     out[4] = fma(om1, g[4], sub(ev, od));
   }
   // diagonal pairs (5,7): e = ux + uy, cx = 1; (6,8): e = uy - ux, cx = -1
   {
     const float w = 1.0f / 36.0f, e = add(ux, uy);
-    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(fb9, e, fx)));
-    const float od = mul(w, fma(or3, e, fb3));
+    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(f.fb9, e, fx)));
+    const float od = fma(c2, add(tx, ty), f.f2);
     out[5] = fma(om1, g[5], add(ev, od));
     out[7] = fma(om1, g[7], sub(ev, od));
   }
   {
     const float w = 1.0f / 36.0f, e = sub(uy, ux);
-    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(-fb9, e, fx)));
-    const float od = mul(w, fma(or3, e, -fb3));
+    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(-f.fb9, e, fx)));
+    const float od = fma(c2, sub(ty, tx), -f.f2);
     out[6] = fma(om1, g[6], add(ev, od));
     out[8] = fma(om1, g[8], sub(ev, od));
   }
   return drho;
+}
+
+// The FP32 collision of one node of run R; field: the node's random-field
+// value, or nullptr under the uniform body force.
+__device__ __forceinline__ float collide_f32_run(const RunDev &R, const float S[9], float P[9],
+                                                 const float *field = nullptr, float feps = 0.f) {
+  if (field) {
+    const F32Force f = f32_force(field_beta_f32(R.f_beta, feps, *field), R.f_cforce);
+    return collide_f32_pairs(S, P, R.f_omega, R.f_om1, R.f_c13, R.f_c2, f);
+  }
+  return collide_f32_pairs(S, P, R.f_omega, R.f_om1, R.f_c13, R.f_c2, R.f_force);
 }
 
 // Drag terms from shifted populations, rest parts removed analytically:

@@ -65,8 +65,7 @@ __device__ __forceinline__ void collide_node(const RunDev &R, const pop_t<F64> S
       collide_ref64(S, P, R.beta, R.wcb, R.omega, R.om1);
     }
   } else {
-    const float beta = map ? field_beta_f32(R.f_beta, R.f_field_eps, *map) : R.f_beta;
-    collide_f32(S, P, beta, R.f_omega, R.f_cforce);
+    collide_f32_run(R, S, P, map, R.f_field_eps);
   }
 }
 
@@ -216,10 +215,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_step_f32(StepArgs a) {
       drho += S[k];
     }
   } else {
-    float beta = R.f_beta;
-    if (R.field_mode && a.step + 1 < R.field_steps && a.maps)
-      beta = field_beta_f32(beta, R.f_field_eps, a.maps[R.map_base + (long long)clone * R.nodes + n]);
-    drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
+    const float *fm = (R.field_mode && a.step + 1 < R.field_steps && a.maps)
+                          ? a.maps + R.map_base + (long long)clone * R.nodes + n
+                          : nullptr;
+    drho = collide_f32_run(R, S, P, fm, R.f_field_eps);
   }
   if (!(drho > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
 #pragma unroll

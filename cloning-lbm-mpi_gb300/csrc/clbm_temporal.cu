@@ -102,11 +102,11 @@ __device__ __forceinline__ void update_general(const TemporalArgs &a, const Band
     if (!(d > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
     return;
   }
-  float beta = R.f_beta;
-  if (R.field_mode && t + 1 < R.field_steps && a.maps)
-    beta = field_beta_f32(beta, R.f_field_eps, a.maps[R.map_base + (long long)b.clone * R.nodes + n]);
+  const float *fm = (R.field_mode && t + 1 < R.field_steps && a.maps)
+                        ? a.maps + R.map_base + (long long)b.clone * R.nodes + n
+                        : nullptr;
   float P[9];
-  const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
+  const float drho = collide_f32_run(R, S, P, fm, R.f_field_eps);
   if (!(drho > -1.0f)) atomicOr(a.err, (unsigned)ERR_BAD_DENSITY);
 #pragma unroll
   for (int k = 0; k < 9; k++) {
@@ -164,12 +164,12 @@ __device__ __forceinline__ void update_general_gather(const TemporalArgs &a, con
     S[k] = ld_cluster(ad[k]);
   }
   if (in_box) store_drag_terms<false>(R, S, x, y, b.clone, terms);
-  float beta = R.f_beta;
   const long long n = (long long)y * W + x;
-  if (R.field_mode && t + 1 < R.field_steps && a.maps)
-    beta = field_beta_f32(beta, R.f_field_eps, a.maps[R.map_base + (long long)b.clone * R.nodes + n]);
+  const float *fm = (R.field_mode && t + 1 < R.field_steps && a.maps)
+                        ? a.maps + R.map_base + (long long)b.clone * R.nodes + n
+                        : nullptr;
   float P[9];
-  const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
+  const float drho = collide_f32_run(R, S, P, fm, R.f_field_eps);
   bad |= !(drho > -1.0f);
 #pragma unroll
   for (int k = 0; k < 9; k++) {
@@ -199,12 +199,12 @@ __device__ __forceinline__ void update_general_local(const TemporalArgs &a, cons
 #pragma unroll
   for (int k = 0; k < 9; k++) S[k] = A[c0 + k];
   if (in_box) store_drag_terms<false>(R, S, x, y, b.clone, terms);
-  float beta = R.f_beta;
   const long long n = (long long)y * W + x;
-  if (R.field_mode && t + 1 < R.field_steps && a.maps)
-    beta = field_beta_f32(beta, R.f_field_eps, a.maps[R.map_base + (long long)b.clone * R.nodes + n]);
+  const float *fm = (R.field_mode && t + 1 < R.field_steps && a.maps)
+                        ? a.maps + R.map_base + (long long)b.clone * R.nodes + n
+                        : nullptr;
   float P[9];
-  const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
+  const float drho = collide_f32_run(R, S, P, fm, R.f_field_eps);
   bad |= !(drho > -1.0f);
 #pragma unroll
   for (int k = 0; k < 9; k++) A[c0 + opp_of(k)] = P[k];
@@ -272,10 +272,8 @@ __device__ __forceinline__ void update_fast(const RunDev &R, float *C, float *U,
 #pragma unroll
     for (int k = 0; k < 9; k++) S[k] = C[o0 + k];
   }
-  float beta = R.f_beta;
-  if (FIELD) beta = field_beta_f32(beta, feps, map[0]);
   float P[9];
-  const float drho = collide_f32_pairs(S, P, beta, R.f_omega, R.f_cforce);
+  const float drho = collide_f32_run(R, S, P, FIELD ? map : nullptr, feps);
   bad |= !(drho > -1.0f);
   if (GATHER) {
     C[o0 + 0] = P[0];
