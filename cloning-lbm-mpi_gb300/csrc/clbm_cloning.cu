@@ -278,14 +278,26 @@ __global__ void __launch_bounds__(CLONE_THREADS) k_clone(DevArrays d, int nruns)
     // draws per marked clone in slot order (generatePerturbedState.cpp:15,
     // drawn at the start of the next interval, :412-416)
     if (R.perturb_mode == 1) {
+      // mrank[j] = marked slots before j (exclusive scan of the marks in slot
+      // order, in the sampling array's space, which is free again); a marked
+      // slot j of rank q is the (mrank[j] - mrank[q*local])-th marked slot of
+      // q's block and takes that many nsnap-blocks further into q's stream
       const int local = nc / R.ranks;
+      // (the marked slots are the killed ones: koff is that scan already)
+      int *mrank = temp;
+      {
+        int o = koff;
+        for (int j = j0; j < j1; j++) {
+          mrank[j] = o;
+          o += ncop[j] == 0;
+        }
+        if (threadIdx.x == 0) mrank[nc] = killed;
+      }
       __syncthreads();
       for (int j = j0; j < j1; j++) {
-        if (!d.mark[g0 + j]) continue;
+        if (ncop[j] != 0) continue;
         const int q = j / local;
-        // marked clones before j within rank q's block
-        int m = 0;
-        for (int i = q * local; i < j; i++) m += d.mark[g0 + i];
+        const int m = mrank[j] - mrank[q * local];
         const uint64_t x = st.d48[q];
         double *p = d.prefactors + (long long)(g0 + j) * MAX_SNAP;
         for (int s = 0; s < R.nsnap; s++)
@@ -294,8 +306,7 @@ __global__ void __launch_bounds__(CLONE_THREADS) k_clone(DevArrays d, int nruns)
       __syncthreads();
       if (threadIdx.x < R.ranks) {
         const int q = threadIdx.x;
-        int cnt = 0;
-        for (int i = q * local; i < (q + 1) * local; i++) cnt += d.mark[g0 + i];
+        const int cnt = mrank[(q + 1) * local] - mrank[q * local];
         st.d48[q] = d48_skip(st.d48[q], (uint64_t)cnt * R.nsnap);
       }
     }

@@ -175,28 +175,33 @@ __global__ void k_ref_perturb_norms(const double *fin, const double *snaps, int 
   }
 }
 
-__global__ void k_ref_perturb_apply(double *fin, const double *snaps, int nsnap, int n,
-                                    const double *pref, const double *partials, int nblocks,
-                                    double eps) {
-  __shared__ double s_w, s_inv;
-  if (threadIdx.x == 0) {
-    double a0 = partials[0], a1 = partials[1];
-    for (int b = 1; b < nblocks; b++) {
-      a0 = DADD(a0, partials[2 * b]);
-      a1 = DADD(a1, partials[2 * b + 1]);
-    }
-    const double weight = DDIV(__dsqrt_rn(a0), __dsqrt_rn(a1));
-    double sum = pref[0];
-    for (int q = 1; q < nsnap; q++) sum = DADD(sum, pref[q]);
-    s_w = weight;
-    s_inv = DDIV(1., DADD(1.0, DMUL(DMUL(sum, eps), weight)));
+// The two norms summed over the blocks' partials in block order, once:
+// out[0] = |f| / |mix| (the mix weight), out[1] = 1 / (1 + eps * sum(pref) * weight)
+// (generatePerturbedState.cpp:22-36).
+__global__ void k_ref_perturb_finalize(const double *pref, int nsnap, const double *partials,
+                                       int nblocks, double eps, double *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double a0 = partials[0], a1 = partials[1];
+  for (int b = 1; b < nblocks; b++) {
+    a0 = DADD(a0, partials[2 * b]);
+    a1 = DADD(a1, partials[2 * b + 1]);
   }
-  __syncthreads();
+  const double weight = DDIV(__dsqrt_rn(a0), __dsqrt_rn(a1));
+  double sum = pref[0];
+  for (int q = 1; q < nsnap; q++) sum = DADD(sum, pref[q]);
+  out[0] = weight;
+  out[1] = DDIV(1., DADD(1.0, DMUL(DMUL(sum, eps), weight)));
+}
+
+// f <- (f + eps * mix * weight) / a with (weight, 1/a) from k_ref_perturb_finalize
+__global__ void k_ref_perturb_apply(double *fin, const double *snaps, int nsnap, int n,
+                                    const double *pref, const double *wa, double eps) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const double w = wa[0], inv = wa[1];
   double mix = DMUL(pref[0], snaps[i]);
   for (int q = 1; q < nsnap; q++) mix = DADD(mix, DMUL(pref[q], snaps[(long long)q * n + i]));
-  fin[i] = DMUL(DADD(fin[i], DMUL(DMUL(eps, mix), s_w)), s_inv);
+  fin[i] = DMUL(DADD(fin[i], DMUL(DMUL(eps, mix), w)), inv);
 }
 
 }  // namespace clbm
@@ -288,13 +293,14 @@ extern "C" int clbm_ref_perturbed_state(double *fin, const double *snaps, double
   cudaStream_t st = (cudaStream_t)stream;
   const int nb = (n + 255) / 256;
   double *d_buf = nullptr;
-  cudaError_t e = cudaMallocAsync(&d_buf, sizeof(double) * (nsnap + 2 * (size_t)nb), st);
+  cudaError_t e = cudaMallocAsync(&d_buf, sizeof(double) * (nsnap + 2 + 2 * (size_t)nb), st);
   if (e != cudaSuccess) return clbm_status_from_cuda(e);
-  double *d_pref = d_buf, *d_part = d_buf + nsnap;
+  double *d_pref = d_buf, *d_wa = d_buf + nsnap, *d_part = d_buf + nsnap + 2;
   e = cudaMemcpyAsync(d_pref, prefactors, sizeof(double) * nsnap, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     k_ref_perturb_norms<<<nb, 256, 0, st>>>(fin, snaps, nsnap, n, d_pref, d_part);
-    k_ref_perturb_apply<<<nb, 256, 0, st>>>(fin, snaps, nsnap, n, d_pref, d_part, nb, eps);
+    k_ref_perturb_finalize<<<1, 32, 0, st>>>(d_pref, nsnap, d_part, nb, eps, d_wa);
+    k_ref_perturb_apply<<<nb, 256, 0, st>>>(fin, snaps, nsnap, n, d_pref, d_wa, eps);
     e = cudaGetLastError();
   }
   cudaFreeAsync(d_buf, st);
@@ -303,10 +309,10 @@ extern "C" int clbm_ref_perturbed_state(double *fin, const double *snaps, double
 }
 
 // ---------------------------------------------------------------------------
-// clbm_ref_perturbed_state_noalloc: the same two kernels as
+// clbm_ref_perturbed_state_noalloc: the same kernels as
 // clbm_ref_perturbed_state, with their scratch (the snapshot prefactors and
-// two norm partial sums per 256 values) in a fixed device array instead of a
-// per-call allocation.  It serves callers that must not allocate device
+// two norm partial sums per 256 values, the mix weight) in a fixed device
+// array instead of a per-call allocation.  It serves callers that must not allocate device
 // memory at all: code running under an allocator that already owns the whole
 // device, or inside a time-critical loop where an allocation's implicit
 // synchronisation is not acceptable.
@@ -315,9 +321,10 @@ constexpr int NOALLOC_MAX_N = 1 << 20;                     // values per state, 
 constexpr int NOALLOC_MAX_BLOCKS = NOALLOC_MAX_N / 256;    // norm partials (pairs)
 constexpr int NOALLOC_PREF = 64;                           // prefactor slots (nsnap <= 64)
 // Shared by every call on a device and kept until the process exits
-// (66 KB per device that loads the library).  Nothing in it has to start at
-// zero: each call overwrites the prefactors and every partial it reads.
-static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_PREF + 2 * NOALLOC_MAX_BLOCKS];
+// (66 KB per device that loads the library): the prefactors, the mix weight
+// and 1/a, then the norm partials.  Nothing in it has to start at zero: each
+// call overwrites the prefactors, the weight pair and every partial it reads.
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_PREF + 2 + 2 * NOALLOC_MAX_BLOCKS];
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mutex;
@@ -361,12 +368,13 @@ extern "C" int clbm_ref_perturbed_state_noalloc(double *fin, const double *snaps
   if (int s = noalloc_scratch(&scratch)) return s;
   cudaStream_t st = (cudaStream_t)stream;
   const int nb = (n + 255) / 256;
-  double *d_pref = scratch, *d_part = scratch + NOALLOC_PREF;
+  double *d_pref = scratch, *d_wa = scratch + NOALLOC_PREF, *d_part = scratch + NOALLOC_PREF + 2;
   cudaError_t e = cudaMemcpyAsync(d_pref, prefactors, sizeof(double) * nsnap,
                                   cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     k_ref_perturb_norms<<<nb, 256, 0, st>>>(fin, snaps, nsnap, n, d_pref, d_part);
-    k_ref_perturb_apply<<<nb, 256, 0, st>>>(fin, snaps, nsnap, n, d_pref, d_part, nb, eps);
+    k_ref_perturb_finalize<<<1, 32, 0, st>>>(d_pref, nsnap, d_part, nb, eps, d_wa);
+    k_ref_perturb_apply<<<nb, 256, 0, st>>>(fin, snaps, nsnap, n, d_pref, d_wa, eps);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

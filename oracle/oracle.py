@@ -22,7 +22,9 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref_core.so"
 REF_DRIVER = HERE / "_ref" / "TLGK_LBM_POPS_PERTURB"
-REF_TREE = Path(os.environ.get("CLBM_REFERENCE_TREE", "/root/reference"))
+# the reference checkout: $CLBM_REFERENCE_TREE, else a checkout named
+# "reference" beside this repository
+REF_TREE = Path(os.environ.get("CLBM_REFERENCE_TREE", str(HERE.parent.parent / "reference")))
 
 W = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
 CX = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])

@@ -1,6 +1,7 @@
 """Regenerate the golden fixtures in tests/golden/ from the REFERENCE itself.
 
-Needs the reference tree (default /root/reference, or $CLBM_REFERENCE_TREE);
+Needs the reference tree ($CLBM_REFERENCE_TREE, else a checkout named
+"reference" beside this repository);
 it compiles the reference's own objects and its pops-perturb driver in place
 (oracle/Makefile -> oracle/_ref/) and records their outputs:
 
