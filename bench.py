@@ -240,6 +240,63 @@ def precision_study(args, wl):
     print(json.dumps(line))
 
 
+def drag_study(args, wl):
+    """Momentum-exchange drag (drag_mode 1) against the reference's stress
+    integration (drag_mode 0) on the same workload, seeds and precision:
+    per run the first interval's drag series (both estimators on the same
+    states), the time-mean drag of every clone over all intervals, the SCGF
+    of each sampler, and the cost of each in ms per interval."""
+    import torch
+    import clbm
+    ctx = {}
+    for name, mode in (("stress", clbm.DRAG_STRESS), ("momentum", clbm.DRAG_MOMENTUM)):
+        descs = wl.descs()
+        for d in descs:
+            d.drag_mode = mode
+        s = clbm.Sampler(descs, wl.precision, max_steps=wl.steps, flags=clbm.FLAG_GRAPH)
+        for i, r in enumerate(wl.runs):
+            s.init_equilibrium(i, r.u0, wl.init_noise, r.seed)
+        if wl.precision == clbm.FP32:
+            s.autotune(launches=3)
+        ctx[name] = s
+    n = args.steps
+    secs = {k: 0.0 for k in ctx}
+    first = {}
+    mean_drag = {k: [np.zeros(r.nclones) for r in wl.runs] for k in ctx}
+    for t in range(n):
+        for k, s in ctx.items():
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.run_interval(wl.steps)
+            s.sync()
+            secs[k] += time.perf_counter() - t0
+            for i in range(len(wl.runs)):
+                dr = s.drag(i)
+                mean_drag[k][i] += dr.mean(axis=1) / n
+                if t == 0:
+                    first[(k, i)] = dr
+            s.clone_step()
+    runs = []
+    for i, r in enumerate(wl.runs):
+        a, b = first[("stress", i)], first[("momentum", i)]
+        dT = wl.steps * r.dt
+        psi = {k: s.scgf(i, dT) for k, s in ctx.items()}
+        ma, mb = mean_drag["stress"][i], mean_drag["momentum"][i]
+        runs.append({"run": i, "k": r.k,
+                     "first_interval": {"mean_stress": float(a.mean()), "mean_momentum": float(b.mean()),
+                                        "rms_rel_diff": float(np.sqrt(np.mean((b - a) ** 2) / np.mean(a ** 2)))},
+                     "time_mean_drag": {"stress": float(ma.mean()), "momentum": float(mb.mean()),
+                                        "rel_diff": float((mb.mean() - ma.mean()) / abs(ma.mean()))},
+                     "scgf": psi,
+                     "scgf_rel_diff": (psi["momentum"] - psi["stress"]) / abs(psi["stress"])})
+    for s in ctx.values():
+        s.close()
+    line = {"study": "drag", "workload": wl.name, "intervals": n, "steps_per_interval": wl.steps,
+            "precision": "fp32" if wl.precision == clbm.FP32 else "fp64", "runs": runs,
+            "ms_per_interval": {k: 1e3 * v / n for k, v in secs.items()}}
+    print(json.dumps(line))
+
+
 def adjoint_study(args, wl, directions: int = 32, every: int = 20, eps: float = 1e-6):
     """Gradient of the interval-integrated drag w.r.t. a Gaussian (sigma =
     1e-4) perturbation of all nine populations: FP32 (and FP64) adjoint
@@ -303,7 +360,9 @@ def main():
     ap.add_argument("--graph", action="store_true", help="replay each interval as a CUDA graph")
     ap.add_argument("--variant", type=int, default=None,
                     help="use this interval kernel variant instead of autotuning (profiling)")
-    ap.add_argument("--study", choices=["precision", "adjoint"], default=None)
+    ap.add_argument("--study", choices=["precision", "adjoint", "drag"], default=None)
+    ap.add_argument("--drag", choices=["stress", "momentum"], default="stress",
+                    help="drag estimator of the weights (stress: the reference's)")
     args = ap.parse_args()
     from clbm import configs
     wl = configs.WORKLOADS[args.workload]()
@@ -317,11 +376,17 @@ def main():
     if args.study == "adjoint":
         adjoint_study(args, wl)
         return
+    if args.study == "drag":
+        drag_study(args, wl)
+        return
 
     import torch
     import clbm
     torch.cuda.set_device(local)
-    s = clbm.Sampler(wl.descs(), wl.precision, max_steps=wl.steps,
+    descs = wl.descs()
+    for d in descs:
+        d.drag_mode = clbm.DRAG_MOMENTUM if args.drag == "momentum" else clbm.DRAG_STRESS
+    s = clbm.Sampler(descs, wl.precision, max_steps=wl.steps,
                      flags=clbm.FLAG_GRAPH if args.graph else 0)
     for i, r in enumerate(wl.runs):
         s.init_equilibrium(i, r.u0, wl.init_noise, r.seed + 1000 * rank)
@@ -431,6 +496,7 @@ def main():
                    "runs": [f"{r.nclones}x{r.width}x{r.height} s={r.side} k={r.k:.3f} tau={r.tau}"
                             for r in wl.runs],
                    "steps_per_interval": wl.steps, "parallelism": f"replicas{world}",
+                   "drag": args.drag,
                    "step_variant": best,
                    "autotune_ms_per_launch": [round(float(x), 4) for x in tune_ms],
                    "l2": "inputs larger than L2 (two population buffers of "

@@ -16,10 +16,11 @@ import numpy as np
 PKG = Path(__file__).resolve().parent.parent
 LIB_PATH = PKG / "_build" / "libclbm.so"
 
-OK, ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_NOMEM, ERR_IO, ERR_TIMEOUT = 0, -1, -2, -3, -4, -5, -6
+OK, ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_NOMEM, ERR_IO = 0, -1, -2, -3, -4, -5
 FP64, FP32 = 0, 1
 RESAMPLE_REFERENCE, RESAMPLE_SYSTEMATIC = 0, 1
 PERTURB_NONE, PERTURB_MIX, PERTURB_UNIFORM = 0, 1, 2
+DRAG_STRESS, DRAG_MOMENTUM = 0, 1
 FLAG_GRAPH = 1
 
 # every entry point include/clbm.h declares, for the export check
@@ -48,7 +49,7 @@ class RunDesc(C.Structure):
         ("tau", C.c_double), ("beta", C.c_double), ("alpha", C.c_double),
         ("force_scale", C.c_double), ("force_shift", C.c_double), ("dt", C.c_double),
         ("perturb_mode", C.c_int), ("resample_mode", C.c_int),
-        ("eps", C.c_double), ("seed", C.c_ulonglong), ("nsnap", C.c_int), ("reserved", C.c_int),
+        ("eps", C.c_double), ("seed", C.c_ulonglong), ("nsnap", C.c_int), ("drag_mode", C.c_int),
         ("field_mode", C.c_int), ("field_steps", C.c_int), ("field_eps", C.c_double),
         ("field_sigma", C.c_double),
     ]

@@ -14,7 +14,9 @@
 // Jacobian is a rank-3 update of (1-omega) I through rho, jx, jy, so its
 // transpose costs three reductions per node.  D is the stress-integration drag
 // (src/lbm_src/force.cpp:8-144) with Pi_xx^neq = sum_{cx!=0} f - rho/3 - jx^2/rho
-// and Pi_xy^neq = f5 - f6 + f7 - f8 - jx jy / rho (its closed form).
+// and Pi_xy^neq = f5 - f6 + f7 - f8 - jx jy / rho (its closed form), or under
+// drag_mode 1 the momentum exchange, linear in S: -2 c_kx on every slot the
+// square bounces back.
 #include "clbm_internal.h"
 #include "clbm_physics.cuh"
 
@@ -49,6 +51,12 @@ __device__ __forceinline__ int adj_locate(const RunDev *runs, int nruns, int &cl
 template <typename T>
 __device__ __forceinline__ void drag_grad(const RunDev &R, int x, int y, const T S[9], T kappa,
                                           T out[9]) {
+  if (R.drag_mode == 1) {
+    const int m = bounce_mask(R, x, y);
+#pragma unroll
+    for (int k = 0; k < 9; k++) out[k] = ((m >> k) & 1) ? kappa * T(-2 * cx_of(k)) : T(0);
+    return;
+  }
   T rho, jx = (S[1] - S[3]) + ((S[5] - S[7]) + (S[8] - S[6]));
   T jy = (S[2] - S[4]) + ((S[5] - S[7]) + (S[6] - S[8]));
   T sum = ((S[0] + (S[1] + S[3])) + (S[2] + S[4])) + ((S[5] + S[7]) + (S[6] + S[8]));

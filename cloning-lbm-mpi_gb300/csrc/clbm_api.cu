@@ -55,6 +55,7 @@ struct clbm_ctx {
   int s_buf = 0;
   int last_steps = 0;
   bool any_mix = false;
+  bool any_stress = false, any_momentum = false;  // drag modes present
   DevArrays d{};
   cudaStream_t stream = nullptr;
   GraphEntry graphs[4];
@@ -101,7 +102,6 @@ extern "C" const char *clbm_strerror(int status) {
     case CLBM_ERR_DEVICE: return "device error word set";
     case CLBM_ERR_NOMEM: return "out of memory";
     case CLBM_ERR_IO: return "I/O error";
-    case CLBM_ERR_TIMEOUT: return "bounded device wait expired";
     default: return "unknown status";
   }
 }
@@ -190,6 +190,10 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
     if (ranks > MAX_RANKS || d.nclones % ranks) return fail(CLBM_ERR_INVALID, "ranks must divide nclones (<= 64)");
     if (d.perturb_mode < 0 || d.perturb_mode > 2) return fail(CLBM_ERR_INVALID, "unknown perturb_mode");
     if (d.resample_mode < 0 || d.resample_mode > 1) return fail(CLBM_ERR_INVALID, "unknown resample_mode");
+    if (d.drag_mode != CLBM_DRAG_STRESS && d.drag_mode != CLBM_DRAG_MOMENTUM)
+      return fail(CLBM_ERR_INVALID, "unknown drag_mode");
+    if (d.drag_mode == CLBM_DRAG_MOMENTUM && (d.xmax - d.xmin < 2 || d.ymax - d.ymin < 2))
+      return fail(CLBM_ERR_INVALID, "momentum-exchange drag needs a square with interior nodes (side >= 3)");
     if (d.perturb_mode == CLBM_PERTURB_MIX && (d.nsnap < 1 || d.nsnap > MAX_SNAP))
       return fail(CLBM_ERR_INVALID, "snapshot mix needs 1 <= nsnap <= 64");
     if (!(d.tau > 0.5)) return fail(CLBM_ERR_INVALID, "tau must exceed 1/2");
@@ -270,6 +274,8 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
     R.f_force = f32_force(R.f_beta, R.f_cforce);
     R.perturb_mode = d.perturb_mode;
     R.resample_mode = d.resample_mode;
+    R.drag_mode = d.drag_mode;
+    (d.drag_mode == CLBM_DRAG_MOMENTUM ? c->any_momentum : c->any_stress) = true;
     R.ranks = d.ranks < 1 ? 1 : d.ranks;
     R.nsnap = d.perturb_mode == CLBM_PERTURB_MIX ? d.nsnap : 0;
     R.seed = d.seed;
@@ -598,7 +604,7 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
     }
   }
   if (prof && (e = cudaEventRecord(e1, s)) != cudaSuccess) return e;
-  if ((e = launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, s)) != cudaSuccess) return e;
+  if ((e = launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, c->any_stress, c->any_momentum, s)) != cudaSuccess) return e;
   if (c->hist_max > 0) {
     if (c->hist_steps == 0) c->hist_steps = steps;
     if (c->hist_steps != steps) c->hist_steps_varied = true;
@@ -1054,7 +1060,7 @@ extern "C" int clbm_drag_fwd(clbm_ctx *c, int steps, int every, double *J) {
                nullptr};
     CK(launch_step(f64, false, a, c->total_blocks, s, c->step_variant));
   }
-  CK(launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, s));
+  CK(launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, c->any_stress, c->any_momentum, s));
   if (J) CK(cudaMemcpyAsync(J, c->d.sacc, sizeof(double) * c->total_clones, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   c->adj.steps = steps;

@@ -26,6 +26,7 @@ __global__ void k_drag_terms_sum(DevArrays d, int nruns, int total_clones) {
   int r = 0;
   while (r + 1 < nruns && g >= d.runs[r + 1].clone_base) r++;
   const RunDev &R = d.runs[r];
+  if (R.drag_mode != 0) return;  // momentum exchange: k_drag_me_sum
   const int c = g - R.clone_base;
   const int nc = R.nclones;
   const int sy = R.ymax - R.ymin + 1, sx = R.xmax - R.xmin + 1;
@@ -47,6 +48,46 @@ __global__ void k_drag_terms_sum(DevArrays d, int nruns, int total_clones) {
   d.drag[(long long)g * d.max_steps + t] = F;
 }
 
+// Momentum-exchange drag of every (clone, step) with a warp-shuffle
+// reduction.  Block (32, 32) for 32 clones of one step: thread (tx, ty) adds
+// the terms ty, ty + 32, ... of clone tx in FP64 (loads coalesced over the
+// clones of the [term][clone] slab); the 32 x 32 partials are transposed
+// through shared memory, so warp ty holds the partials of clone ty in its
+// lanes, and an xor butterfly (offsets 16, 8, 4, 2, 1) completes the sum in a
+// fixed order (the oracle restates the same order).
+template <bool F64>
+__global__ void __launch_bounds__(1024) k_drag_me_sum(DevArrays d, int nruns, int total_clones) {
+  using T = typename std::conditional<F64, double, float>::type;
+  __shared__ double part[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y, t = blockIdx.y;
+  const int g = blockIdx.x * 32 + tx;
+  double v = 0.0;
+  if (g < total_clones) {
+    int r = 0;
+    while (r + 1 < nruns && g >= d.runs[r + 1].clone_base) r++;
+    const RunDev &R = d.runs[r];
+    if (R.drag_mode == 1) {
+      const int nc = R.nclones;
+      const T *tt = (const T *)d.terms + (long long)t * d.term_slab + R.term_base + (g - R.clone_base);
+      for (int i = ty; i < R.nterms; i += 32) v = DADD(v, (double)tt[(long long)i * nc]);
+    }
+  }
+  part[ty][tx] = v;
+  __syncthreads();
+  double w = part[tx][ty];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) w = DADD(w, __shfl_xor_sync(0xffffffffu, w, o));
+  const int gc = blockIdx.x * 32 + ty;
+  if (tx != 0 || gc >= total_clones) return;
+  int r = 0;
+  while (r + 1 < nruns && gc >= d.runs[r + 1].clone_base) r++;
+  const RunDev &R = d.runs[r];
+  if (R.drag_mode != 1) return;
+  const double F = DSUB(DMUL(w, R.force_scale), R.force_shift);
+  if (!isfinite(F)) atomicOr(d.err, (unsigned)ERR_NONFINITE_DRAG);
+  d.drag[(long long)gc * d.max_steps + t] = F;
+}
+
 __global__ void k_drag_integrate(DevArrays d, int nruns, int total_clones, int steps) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= total_clones) return;
@@ -59,14 +100,25 @@ __global__ void k_drag_integrate(DevArrays d, int nruns, int total_clones, int s
 }
 
 cudaError_t launch_drag_reduce(bool f64, const DevArrays &d, int nruns, int total_clones,
-                               int steps, cudaStream_t s) {
-  dim3 grid((total_clones + 127) / 128, steps);
-  if (f64)
-    k_drag_terms_sum<true><<<grid, 128, 0, s>>>(d, nruns, total_clones);
-  else
-    k_drag_terms_sum<false><<<grid, 128, 0, s>>>(d, nruns, total_clones);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+                               int steps, bool stress, bool momentum, cudaStream_t s) {
+  if (stress) {
+    dim3 grid((total_clones + 127) / 128, steps);
+    if (f64)
+      k_drag_terms_sum<true><<<grid, 128, 0, s>>>(d, nruns, total_clones);
+    else
+      k_drag_terms_sum<false><<<grid, 128, 0, s>>>(d, nruns, total_clones);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (momentum) {
+    dim3 grid((total_clones + 31) / 32, steps), block(32, 32);
+    if (f64)
+      k_drag_me_sum<true><<<grid, block, 0, s>>>(d, nruns, total_clones);
+    else
+      k_drag_me_sum<false><<<grid, block, 0, s>>>(d, nruns, total_clones);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   k_drag_integrate<<<(total_clones + 127) / 128, 128, 0, s>>>(d, nruns, total_clones, steps);
   return cudaGetLastError();
 }

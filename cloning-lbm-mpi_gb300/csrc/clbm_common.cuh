@@ -31,7 +31,6 @@ enum : unsigned {
   ERR_BAD_DENSITY = 1u << 2,
   ERR_BAD_PARENT = 1u << 3,
   ERR_RESAMPLE = 1u << 4,
-  ERR_TIMEOUT = 1u << 5,
 };
 
 // Body-force terms of the FP32 collision for one value of beta:
@@ -70,7 +69,7 @@ struct RunDev {
   int nterms;                  // drag terms per clone per step
   int nodes;                   // W*H
   unsigned div_w;              // ceil(2^32 / W): y = umulhi(n, div_w)
-  int pad_;
+  int drag_mode;               // 0 stress integration, 1 momentum exchange
   // tile tables of the FP32 step for tiles of 128 / 256 / 512 nodes: first
   // block of this run, tiles per clone and ceil(2^32 / tiles)
   int tile_base[3];

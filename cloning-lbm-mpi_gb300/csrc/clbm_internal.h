@@ -115,7 +115,7 @@ cudaError_t launch_perturb_norms(bool f64, const RunDev *runs, int nruns, const 
                                  const double *snaps, double *partials, double *pert,
                                  int blocks, int total_clones, cudaStream_t s);
 cudaError_t launch_drag_reduce(bool f64, const DevArrays &d, int nruns, int total_clones,
-                               int steps, cudaStream_t s);
+                               int steps, bool stress, bool momentum, cudaStream_t s);
 cudaError_t launch_clone(const DevArrays &d, int nruns, cudaStream_t s);
 cudaError_t launch_adj_init(bool f64, const RunDev *runs, int nruns, const void *P, void *sigma,
                             int blocks, cudaStream_t s);

@@ -245,17 +245,54 @@ __device__ __forceinline__ void pi_f32(const float g[9], float &drho_o, float &p
   pxy = fma(-rux, uy, sub(a57, a68));
 }
 
+// Momentum-exchange drag of one perimeter node.  A slot k that the square
+// bounces back holds S(n,k) = P(n, opp k): the population that left n towards
+// the solid along c_{opp k} and came back along c_k, handing the body
+// c_{opp k} P - c_k S = -2 c_k S of momentum.  The x parts are summed in k
+// order (c_kx = 0 slots carry none).  FP64 on f; FP32 on the shifted g, whose
+// missing rest parts -2 c_kx w_k cancel over the perimeter (West against East
+// row by row, corner against corner, +-c_x pairs on North and South).
+template <bool F64>
+__device__ __forceinline__ typename std::conditional<F64, double, float>::type me_node_term(
+    const typename std::conditional<F64, double, float>::type S[9], int mask) {
+  typename std::conditional<F64, double, float>::type v = 0;
+#pragma unroll
+  for (int k = 1; k < 9; k++) {
+    if (cx_of(k) == 0 || !((mask >> k) & 1)) continue;
+    if constexpr (F64) {
+      const double s2 = DADD(S[k], S[k]);
+      v = cx_of(k) < 0 ? DADD(v, s2) : DSUB(v, s2);
+    } else {
+      const float s2 = __fadd_rn(S[k], S[k]);
+      v = cx_of(k) < 0 ? __fadd_rn(v, s2) : __fsub_rn(v, s2);
+    }
+  }
+  return v;
+}
+
 // Drag terms of one perimeter node, stored at [term][clone] so that the
 // reduction reads them coalesced: West (x = xmin, index y - ymin), East,
-// North (y = ymax, index x - xmin), South.  FP64: the reference's per-node
-// expressions (force.cpp:48, :78, :108, :138).  FP32: shifted variant without
-// the +-1/3 that cancel between West and East.
+// North (y = ymax, index x - xmin), South.  Stress integration (drag_mode 0):
+// FP64 the reference's per-node expressions (force.cpp:48, :78, :108, :138),
+// FP32 a shifted variant without the +-1/3 that cancel between West and East.
+// Momentum exchange (drag_mode 1): the node's me_node_term in its West or
+// East slot (corners included) or its North or South slot, 0 in the North and
+// South slots of the corners, so every node counts once.
 template <bool F64>
 __device__ __forceinline__ void store_drag_terms(
     const RunDev &R, const typename std::conditional<F64, double, float>::type S[9], int x, int y,
     int clone, typename std::conditional<F64, double, float>::type *T) {
   const int sy = R.ymax - R.ymin, sx = R.xmax - R.xmin;
   const int nc = R.nclones;
+  if (R.drag_mode == 1) {
+    const auto v = me_node_term<F64>(S, bounce_mask(R, x, y));
+    const bool corner_x = x == R.xmin || x == R.xmax;
+    if (x == R.xmin) T[(long long)(y - R.ymin) * nc + clone] = v;
+    if (x == R.xmax) T[(long long)(sy + 1 + y - R.ymin) * nc + clone] = v;
+    if (y == R.ymax) T[(long long)(2 * (sy + 1) + x - R.xmin) * nc + clone] = corner_x ? 0 : v;
+    if (y == R.ymin) T[(long long)(2 * (sy + 1) + sx + 1 + x - R.xmin) * nc + clone] = corner_x ? 0 : v;
+    return;
+  }
   typename std::conditional<F64, double, float>::type west, east, north, south;
   if constexpr (F64) {
     double rho, pxx, pxy;

@@ -41,7 +41,6 @@ extern "C" {
 #define CLBM_ERR_DEVICE (-3)  /* the device error word was set (see below) */
 #define CLBM_ERR_NOMEM (-4)   /* device or pinned host allocation failed */
 #define CLBM_ERR_IO (-5)      /* file I/O (drivers) */
-#define CLBM_ERR_TIMEOUT (-6) /* a bounded device wait gave up */
 
 /* device error word bits (clbm_error_word) */
 #define CLBM_DEV_NONFINITE_DRAG 0x1u  /* a drag value was NaN or Inf */
@@ -49,7 +48,6 @@ extern "C" {
 #define CLBM_DEV_BAD_DENSITY 0x4u     /* rho <= 0 or NaN at some node */
 #define CLBM_DEV_BAD_PARENT 0x8u      /* resampling produced an invalid parent */
 #define CLBM_DEV_RESAMPLE 0x10u       /* copy numbers could not be corrected */
-#define CLBM_DEV_TIMEOUT 0x20u        /* a bounded spin-wait expired */
 
 /* arithmetic of the populations */
 #define CLBM_FP64 0 /* FP64, reference operation order, no fused multiply-add */
@@ -62,6 +60,15 @@ extern "C" {
                                       random streams emulated bit for bit */
 #define CLBM_RESAMPLE_SYSTEMATIC 1 /* systematic resampling, one Philox uniform
                                       per interval, log-domain weights */
+
+/* drag on the square, the observable of the weights (clbm_run_desc.drag_mode) */
+#define CLBM_DRAG_STRESS 0   /* the reference's stress integration over the
+                                perimeter nodes (src/lbm_src/force.cpp:8-144) */
+#define CLBM_DRAG_MOMENTUM 1 /* momentum exchange of the links bounced back on
+                                the square: F = sum -2 c_kx f_k over the slots
+                                the square reflects (no counterpart in the
+                                reference; a different estimator of the same
+                                force, see clbm_run_interval) */
 
 /* perturbation of newly created clones (at the start of the next interval) */
 #define CLBM_PERTURB_NONE 0
@@ -93,7 +100,7 @@ typedef struct {
   double eps;                 /* perturbation amplitude */
   unsigned long long seed;    /* counter-based random streams */
   int nsnap;                  /* snapshots for CLBM_PERTURB_MIX (<= 64) */
-  int reserved;
+  int drag_mode;              /* CLBM_DRAG_* (0: the reference's) */
   /* spatially random body force of the forcing variant
    * (src/mpi_LBM_GK_forcing.cpp:333-364): at the start of every interval
    * each clone draws a Gaussian random field `map` with covariance
@@ -160,8 +167,9 @@ int clbm_ref_perturbed_state(double *fin, const double *snaps, double eps,
  * values of one state, 9*Dx*Dy) is limited to 1048576 and nsnap to 64; larger
  * sizes return CLBM_ERR_INVALID.  The first call on a device looks up the
  * array's device address, so make that first call before any stream capture.
- * All calls share the array: calls that overlap on the GPU (other streams,
- * other host threads) race and must be serialised by the caller. */
+ * Each call synchronises `stream` before it returns.  All calls share the
+ * array: calls that overlap on the GPU (other streams, other host threads)
+ * race and must be serialised by the caller. */
 int clbm_ref_perturbed_state_noalloc(double *fin, const double *snaps,
                                      double eps, int nsnap, int n,
                                      const double *prefactors, void *stream);
@@ -209,7 +217,11 @@ int clbm_init_equilibrium(clbm_ctx *ctx, int run, double u0, double noise,
 /* one cloning interval of `steps` LB steps for every clone of every run:
  * pending perturbation of new clones, then per step stream-collide with wall
  * and square bounce-back and interior reset, the drag on the square after
- * every step, and the weight integral s_j = dt * sum F (pops driver :399-469). */
+ * every step, and the weight integral s_j = dt * sum F (pops driver :399-469).
+ * The drag F is the run's drag_mode: the reference's stress integration, or
+ * the momentum exchange of the links the square bounces back, evaluated in
+ * the same pass from the populations the step already holds in registers and
+ * summed per clone by a warp-shuffle reduction in a fixed order. */
 int clbm_run_interval(clbm_ctx *ctx, int steps);
 /* drag series of the last interval, [nclones][steps] F values of a run */
 int clbm_get_drag(clbm_ctx *ctx, int run, double *out);

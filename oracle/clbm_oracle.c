@@ -198,6 +198,45 @@ double orc_force_on_square(const orc_geom *g, const double *f, double omega) {
   return west + east + north + south;
 }
 
+/* Momentum exchange (no counterpart in the reference; libclbm's
+ * CLBM_DRAG_MOMENTUM).  A slot k the square bounces back holds the
+ * post-collision population that left the node along c_{opp k}, reflected, so
+ * the link hands the body -2 c_k f_k of momentum; x parts in k order. */
+static double me_node(const orc_geom *g, const double *f, int x, int y) {
+  const int m = orc_bounce_mask(g, x, y);
+  double v = 0.0;
+  for (int k = 1; k < 9; k++) {
+    if (CX[k] == 0 || !((m >> k) & 1)) continue;
+    const double s2 = f[AOS(g, x, y, k)] + f[AOS(g, x, y, k)];
+    v = CX[k] < 0 ? v + s2 : v - s2;
+  }
+  return v;
+}
+
+double orc_force_momentum_exchange(const orc_geom *g, const double *f) {
+  const int sy = g->ymax - g->ymin + 1, sx = g->xmax - g->xmin + 1;
+  const int nt = 2 * sy + 2 * sx;
+  double *term = (double *)malloc(sizeof(double) * nt);
+  int i = 0;
+  for (int y = g->ymin; y <= g->ymax; y++) term[i++] = me_node(g, f, g->xmin, y);
+  for (int y = g->ymin; y <= g->ymax; y++) term[i++] = me_node(g, f, g->xmax, y);
+  for (int x = g->xmin; x <= g->xmax; x++)
+    term[i++] = (x == g->xmin || x == g->xmax) ? 0.0 : me_node(g, f, x, g->ymax);
+  for (int x = g->xmin; x <= g->xmax; x++)
+    term[i++] = (x == g->xmin || x == g->xmax) ? 0.0 : me_node(g, f, x, g->ymin);
+  double lane[32], next[32];
+  for (int l = 0; l < 32; l++) {
+    lane[l] = 0.0;
+    for (int j = l; j < nt; j += 32) lane[l] += term[j];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    for (int l = 0; l < 32; l++) next[l] = lane[l] + lane[l ^ o];
+    memcpy(lane, next, sizeof lane);
+  }
+  free(term);
+  return lane[0];
+}
+
 void orc_lbm_step(const orc_geom *g, double **state, double **scratch,
                   double *rho, double *ux, double *uy, double beta,
                   const double *map, double tau, double eps) {
@@ -574,7 +613,8 @@ int orc_run_sampler(const orc_sampler_cfg *cfg, double *states,
       for (int tt = 0; tt < cfg->steps; tt++) {
         orc_lbm_step(g, &cur, &tmp, NULL, NULL, NULL, cfg->beta, NULL,
                      cfg->tau, 0.0);
-        double F = orc_force_on_square(g, cur, omega);
+        double F = cfg->drag_mode == 1 ? orc_force_momentum_exchange(g, cur)
+                                       : orc_force_on_square(g, cur, omega);
         F = F * cfg->force_scale;
         F = F - cfg->force_shift;
         if (drag) drag[((size_t)t * nc + j) * cfg->steps + tt] = F;

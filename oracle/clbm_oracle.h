@@ -38,6 +38,12 @@ void orc_walls_bb(const orc_geom *g, double *fout, const double *fin);
 void orc_square_bb(const orc_geom *g, double *fout, const double *fin);
 void orc_interior_reset(const orc_geom *g, double *fout);
 double orc_force_on_square(const orc_geom *g, const double *f, double omega);
+/* momentum-exchange x-drag on the square of a streamed, bounced state f:
+ * per perimeter node sum_k -2 c_kx f_k over the slots the square bounces
+ * back, nodes in the West, East, North, South order of the stress
+ * integration (corners in West / East), summed as 32 strided lane partials
+ * followed by an xor butterfly (the libclbm momentum-exchange reduction). */
+double orc_force_momentum_exchange(const orc_geom *g, const double *f);
 /* one full LB step as the drivers chain it; *state and *scratch are swapped */
 void orc_lbm_step(const orc_geom *g, double **state, double **scratch,
                   double *rho, double *ux, double *uy, double beta,
@@ -96,6 +102,7 @@ typedef struct {
   double eps;
   uint64_t seed;
   uint32_t run;
+  int drag_mode; /* 0 stress integration (the reference), 1 momentum exchange */
 } orc_sampler_cfg;
 int orc_run_sampler(const orc_sampler_cfg *cfg, double *states,
                     const double *snaps, double *drag, int *labels,

@@ -41,7 +41,8 @@ class SamplerCfg(C.Structure):
                 ("ranks", C.c_int), ("tau", C.c_double), ("beta", C.c_double),
                 ("alpha", C.c_double), ("force_scale", C.c_double), ("force_shift", C.c_double),
                 ("dt", C.c_double), ("perturb_mode", C.c_int), ("resample_mode", C.c_int),
-                ("nsnap", C.c_int), ("eps", C.c_double), ("seed", C.c_uint64), ("run", C.c_uint32)]
+                ("nsnap", C.c_int), ("eps", C.c_double), ("seed", C.c_uint64), ("run", C.c_uint32),
+                ("drag_mode", C.c_int)]
 
 
 class D48(C.Structure):
@@ -82,6 +83,7 @@ def lib() -> C.CDLL:
             build()
         L = C.CDLL(str(LIB))
         L.orc_force_on_square.restype = C.c_double
+        L.orc_force_momentum_exchange.restype = C.c_double
         L.orc_drand48_next.restype = C.c_double
         L.orc_glibc_rand_next.restype = C.c_int32
         L.orc_philox_uniform.restype = C.c_double
@@ -187,6 +189,12 @@ def force(g: Geom, f: np.ndarray, omega: float) -> float:
     return lib().orc_force_on_square(C.byref(g), _p(f), C.c_double(omega))
 
 
+def force_momentum_exchange(g: Geom, f: np.ndarray) -> float:
+    """Momentum-exchange x-drag of a streamed, bounced AoS state."""
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    return lib().orc_force_momentum_exchange(C.byref(g), _p(f))
+
+
 def run_clone(g: Geom, f: np.ndarray, steps: int, beta: float, tau: float) -> tuple[np.ndarray, np.ndarray]:
     """steps reference LB steps of one clone with the drag after each."""
     drag = np.empty(steps)
@@ -213,11 +221,11 @@ def run_sampler(g: Geom, states: np.ndarray, *, steps: int, intervals: int, tau:
                 beta: float, alpha: float, force_scale: float, force_shift: float, dt: float,
                 perturb_mode: int = 0, resample_mode: int = 0, eps: float = 0.0,
                 snaps: np.ndarray | None = None, seed: int = 0, run: int = 0,
-                ranks: int = 1) -> dict:
+                ranks: int = 1, drag_mode: int = 0) -> dict:
     nc = states.size // (9 * g.nx * g.ny)
     nsnap = 0 if snaps is None else snaps.size // (9 * g.nx * g.ny)
     cfg = SamplerCfg(g, nc, steps, intervals, ranks, tau, beta, alpha, force_scale, force_shift,
-                     dt, perturb_mode, resample_mode, nsnap, eps, seed, run)
+                     dt, perturb_mode, resample_mode, nsnap, eps, seed, run, drag_mode)
     st = np.ascontiguousarray(states, dtype=np.float64).copy()
     drag = np.zeros((intervals, nc, steps))
     labels = np.zeros((intervals, nc), np.int32)

@@ -31,9 +31,12 @@ def test_forward_drag_matches_oracle(gpu, clbm_lib, orc):
         assert np.array_equal(s.dump(0, 1), states[g.nx * g.ny * 9:2 * g.nx * g.ny * 9])  # state untouched
 
 
+@pytest.mark.parametrize("drag_mode", [0, 1])
 @pytest.mark.parametrize("prec,tol", [(0, 1e-6), (1, 2e-3)])
-def test_adjoint_vs_central_differences(gpu, clbm_lib, orc, prec, tol):
+def test_adjoint_vs_central_differences(gpu, clbm_lib, orc, prec, tol, drag_mode):
+    """drag_mode 0: the reference's stress integration; 1: momentum exchange."""
     g, phys, d = case(orc, clbm_lib)
+    d.drag_mode = drag_mode
     nc, T, every, eps = 3, 30, 7, 1e-6
     n = 9 * g.nx * g.ny
     rng = np.random.default_rng(5)
