@@ -427,13 +427,22 @@ def main():
     step_s = step_ms / 1e3 / max(1, nsteps)
     achieved = bpl * nodes_total / step_s / 1e9
     peak, peak_kind = hbm_peak()
-    vinfo = clbm.describe_variant(best) if wl.precision == clbm.FP32 else \
-        {"kind": "streaming", "kernel": "k_step_f64", "variant": 0}
-    cluster = vinfo["kind"] == "cluster-resident"
+    if wl.precision == clbm.FP32:
+        kinds = [clbm.describe_variant(int(v)) for v in s.run_variants()]
+    else:
+        kinds = [{"kind": "streaming", "kernel": "k_step_f64", "variant": 0}] * len(wl.runs)
+    n_cluster = sum(k["kind"] == "cluster-resident" for k in kinds)
+    any_stream = n_cluster < len(kinds)
+    if all(k == kinds[0] for k in kinds):
+        vinfo = kinds[0]
+    else:  # per-run plan: cluster-resident runs concurrent with the streaming ones
+        vinfo = {"kind": "per-run", "kernel": "k_temporal_f32+k_step_f32", "variant": best, "runs": kinds}
+    cluster = n_cluster > 0
     # DRAM bytes per launch of the dominant kernel (one step for the streaming
     # kernel, one interval of wl.steps steps for the cluster-resident one)
     traffic = ncu_traffic(f"{vinfo['kernel']}_{args.workload}.md")
-    launches_per_interval = (len(wl.runs) if cluster else wl.steps) + 4
+    # reseed + the interval kernels + drag reduction (2) + cloning step
+    launches_per_interval = n_cluster + (wl.steps if any_stream else 0) + 4
     # the streaming step kernel's own roofline, from the autotuner's timing of
     # its best launch variant on this workload (one launch per step)
     stream_ref = None

@@ -22,6 +22,7 @@ RESAMPLE_REFERENCE, RESAMPLE_SYSTEMATIC = 0, 1
 PERTURB_NONE, PERTURB_MIX, PERTURB_UNIFORM = 0, 1, 2
 DRAG_STRESS, DRAG_MOMENTUM = 0, 1
 FLAG_GRAPH = 1
+VARIANT_PER_RUN = -1
 
 # every entry point include/clbm.h declares, for the export check
 EXPORTS = [
@@ -32,7 +33,7 @@ EXPORTS = [
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
-    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant", "clbm_shard_plan", "clbm_ref_random_field",
+    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant", "clbm_set_run_variants", "clbm_get_run_variants", "clbm_shard_plan", "clbm_ref_random_field",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -108,6 +109,8 @@ def lib() -> C.CDLL:
         L.clbm_profile.argtypes = [vp, i]
         L.clbm_autotune.argtypes = [vp, i, C.POINTER(i), vp, C.POINTER(i)]
         L.clbm_set_step_variant.argtypes = [vp, i]
+        L.clbm_set_run_variants.argtypes = [vp, vp]
+        L.clbm_get_run_variants.argtypes = [vp, vp]
         L.clbm_profile_read.argtypes = [vp, C.POINTER(d), C.POINTER(i)]
         L.clbm_error_word.argtypes = [vp, C.POINTER(C.c_uint), i]
         L.clbm_sync.argtypes = [vp]
@@ -379,6 +382,15 @@ class Sampler:
 
     def set_step_variant(self, v: int):
         check(lib().clbm_set_step_variant(self.h, v), "clbm_set_step_variant")
+
+    def set_run_variants(self, variants):
+        a = np.ascontiguousarray(variants, dtype=np.int32)
+        check(lib().clbm_set_run_variants(self.h, _p(a)), "clbm_set_run_variants")
+
+    def run_variants(self) -> np.ndarray:
+        a = np.zeros(len(self.runs), np.int32)
+        check(lib().clbm_get_run_variants(self.h, _p(a)), "clbm_get_run_variants")
+        return a
 
     def profile(self, enable: bool):
         check(lib().clbm_profile(self.h, int(enable)), "clbm_profile")

@@ -70,8 +70,17 @@ struct clbm_ctx {
   int max_nodes = 0;
   int total_tiles[3] = {0, 0, 0};
   int step_variant = 0;  // FP32 step launch variant (clbm_autotune)
-  int temporal_cs = 0;   // > 0: FP32 intervals run cluster-resident with this cluster size
-  int temporal_variant = 0;
+  // interval kernel of each run (FP32): cluster size of the cluster-resident
+  // kernel, 0 = the streaming step kernel, and its thread variant.  The
+  // streaming runs share one step launch per step; every cluster-resident run
+  // is one launch per interval on its own side stream, concurrent with them.
+  std::vector<int> run_cs, run_tv;
+  bool stream_subset = false;       // some runs are cluster-resident: step the rest through...
+  RunDev *d_runs_stream = nullptr;  // ...this table (their descriptors, own tile bases)
+  std::vector<RunDev> stream_h;
+  int stream_nruns = 0, stream_tiles[3] = {0, 0, 0};
+  std::vector<cudaStream_t> side;   // side stream i carries the i-th cluster-resident run
+  std::vector<cudaEvent_t> fork_join;  // [0] fork, [1 + i] side stream i done
   bool pending = false;  // a clone step's copies/perturbations await the next interval
   // random body-force fields (forcing variant)
   bool any_field = false;
@@ -155,7 +164,9 @@ static void destroy_graphs(clbm_ctx *c) {
 extern "C" int clbm_destroy(clbm_ctx *c) {
   if (!c) return CLBM_OK;
   destroy_graphs(c);
-  void *bufs[] = {c->pop[0], c->pop[1], c->d.runs, c->d.state, c->d.sacc, c->d.drag, c->d.weights,
+  for (cudaStream_t t : c->side) cudaStreamDestroy(t);
+  for (cudaEvent_t e : c->fork_join) cudaEventDestroy(e);
+  void *bufs[] = {c->d_runs_stream, c->pop[0], c->pop[1], c->d.runs, c->d.state, c->d.sacc, c->d.drag, c->d.weights,
                   c->d.labels, c->d.mark, c->d.copies_pre, c->d.copies_post, c->d.prefactors,
                   c->d.pert, c->d.partials, c->d.scratch_i, c->d.scratch_d, c->d.snaps,
                   c->d.rvalues, c->d.logr, c->d.err, c->d.terms, c->d_identity, c->d_zeros,
@@ -365,6 +376,10 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
   for (int b = 0; b < 2; b++)
     if ((e = cudaMalloc(&c->pop[b], c->pop_elems * c->elem_size)) != cudaSuccess) return bail(e);
   DevArrays &D = c->d;
+  c->run_cs.assign(nruns, 0);
+  c->run_tv.assign(nruns, 0);
+  c->stream_nruns = nruns;
+  if ((e = dalloc(c->d_runs_stream, nruns)) != cudaSuccess) return bail(e);
   if ((e = dalloc(D.runs, nruns)) != cudaSuccess) return bail(e);
   if ((e = dalloc(D.state, nruns)) != cudaSuccess) return bail(e);
   if ((e = dalloc(D.sacc, clones)) != cudaSuccess) return bail(e);
@@ -544,6 +559,129 @@ extern "C" int clbm_init_equilibrium(clbm_ctx *c, int run, double u0, double noi
   return clbm_status_from_cuda(e);
 }
 
+// ---------------------------------------------------------------------------
+// The LB steps of an interval under a plan: which runs the streaming step
+// kernel advances (through which descriptor table) and which run
+// cluster-resident, with which cluster size and thread count.
+struct LbPlan {
+  std::vector<int> cs, tv;        // per run: cluster size (0 = streaming), thread variant
+  std::vector<char> active;       // runs to advance (autotuner timing of one run); empty = all
+  const RunDev *table = nullptr;  // step-kernel table of the streaming runs
+  int nstream = 0, tiles[3] = {0, 0, 0}, variant = 0;
+};
+
+static bool plan_active(const LbPlan &p, int r) { return p.active.empty() || p.active[r]; }
+
+static LbPlan current_plan(const clbm_ctx *c, bool f64) {
+  LbPlan p;
+  p.cs = f64 ? std::vector<int>(c->nruns, 0) : c->run_cs;
+  p.tv = c->run_tv;
+  const bool sub = !f64 && c->stream_subset;
+  p.table = sub ? c->d_runs_stream : c->d.runs;
+  p.nstream = sub ? c->stream_nruns : c->nruns;
+  for (int q = 0; q < 3; q++) p.tiles[q] = sub ? c->stream_tiles[q] : c->total_tiles[q];
+  p.variant = c->step_variant;
+  return p;
+}
+
+// The streaming runs' own step-kernel table: their descriptors with tile
+// bases counted over these runs only (the grid covers just their tiles).
+static cudaError_t upload_stream_table(clbm_ctx *c, const std::vector<int> &runs) {
+  c->stream_h.clear();
+  int tiles[3] = {0, 0, 0};
+  for (int r : runs) {
+    RunDev R = c->runs_h[r];
+    for (int q = 0; q < 3; q++) {
+      R.tile_base[q] = tiles[q];
+      tiles[q] += R.nclones * R.tiles[q];
+    }
+    c->stream_h.push_back(R);
+  }
+  for (int q = 0; q < 3; q++) c->stream_tiles[q] = tiles[q];
+  c->stream_nruns = (int)runs.size();
+  if (runs.empty()) return cudaSuccess;
+  // pageable source: the copy is staged before the call returns
+  return cudaMemcpyAsync(c->d_runs_stream, c->stream_h.data(), sizeof(RunDev) * runs.size(),
+                         cudaMemcpyHostToDevice, c->stream);
+}
+
+static cudaError_t ensure_side(clbm_ctx *c, int n) {
+  while ((int)c->side.size() < n) {
+    cudaStream_t t = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    c->side.push_back(t);
+  }
+  while ((int)c->fork_join.size() < n + 1) {
+    cudaEvent_t ev = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return e;
+    c->fork_join.push_back(ev);
+  }
+  return cudaSuccess;
+}
+
+// Enqueue `steps` LB steps of the plan's runs.  Interval: P_0 in buffer src,
+// S_T left in buffer dst; the streaming runs alternate between the two
+// buffers as the pull scheme does and store S on their last step.  timing
+// (autotuner): every streaming launch reads src and writes the other buffer
+// and none is a last step, so the state in src is left untouched.
+static cudaError_t enqueue_lb_steps(clbm_ctx *c, const LbPlan &p, int steps, int src, int dst, bool timing) {
+  const bool f64 = c->precision == CLBM_FP64;
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+  int nside = 0;
+  for (int r = 0; r < c->nruns; r++) nside += p.cs[r] > 0 && plan_active(p, r);
+  if (nside) {
+    if ((e = ensure_side(c, nside)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(c->fork_join[0], s)) != cudaSuccess) return e;
+  }
+  int i = 0;
+  for (int r = 0; r < c->nruns; r++) {
+    if (!(p.cs[r] > 0 && plan_active(p, r))) continue;
+    const RunDev &R = c->runs_h[r];
+    cudaStream_t ts = c->side[i];
+    if ((e = cudaStreamWaitEvent(ts, c->fork_join[0], 0)) != cudaSuccess) return e;
+    TemporalArgs ta{R, r, steps, (const float *)c->pop[src], (float *)c->pop[dst], (float *)c->d.terms,
+                    c->d.term_slab, c->d.err, c->d_maps};
+    if ((e = launch_temporal(ta, p.cs[r], p.tv[r], R.nclones, R.W, R.H, ts)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(c->fork_join[1 + i], ts)) != cudaSuccess) return e;
+    i++;
+  }
+  if (p.nstream > 0) {
+    int cur = src;
+    for (int t = 0; t < steps; t++) {
+      StepArgs a{p.table, p.nstream, t, c->pop[cur], c->pop[1 - cur], c->d.terms, c->d.term_slab,
+                 c->d.err, c->total_clones, c->max_nodes, {p.tiles[0], p.tiles[1], p.tiles[2]}, c->d_maps};
+      if ((e = launch_step(f64, !timing && t == steps - 1, a, c->total_blocks, s, p.variant)) != cudaSuccess)
+        return e;
+      if (!timing) cur = 1 - cur;
+    }
+  }
+  for (int k = 0; k < nside; k++)
+    if ((e = cudaStreamWaitEvent(s, c->fork_join[1 + k], 0)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+// Install a plan: per run cluster size (0 = streaming) and thread variant,
+// the streaming runs' launch variant.  Captured intervals are dropped.
+static cudaError_t set_plan(clbm_ctx *c, const std::vector<int> &cs, const std::vector<int> &tv, int variant) {
+  c->run_cs = cs;
+  c->run_tv = tv;
+  c->step_variant = variant;
+  std::vector<int> streaming;
+  for (int r = 0; r < c->nruns; r++)
+    if (!cs[r]) streaming.push_back(r);
+  c->stream_subset = (int)streaming.size() != c->nruns;
+  cudaError_t e = cudaSuccess;
+  if (c->stream_subset)
+    e = upload_stream_table(c, streaming);
+  else
+    c->stream_nruns = c->nruns;
+  destroy_graphs(c);
+  return e;
+}
+
 // Enqueue one interval on the context's stream (no synchronisation).
 // prof: record an event pair around the step launches (eager mode only).
 static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof = false) {
@@ -565,8 +703,6 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
   ReseedArgs ra{c->d.runs, c->nruns, S, c->pop[1 - sbuf], c->d.labels, c->d.mark, c->d.pert,
                 c->d.prefactors, c->d.snaps, c->d.state, c->d.err, c->d_maps};
   if ((e = launch_reseed(f64, ra, c->total_blocks, s)) != cudaSuccess) return e;
-  int cur = 1 - sbuf;
-  const bool temporal = !f64 && c->temporal_cs > 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (prof) {
     if ((size_t)c->ev_used + 2 > c->ev.size()) {
@@ -582,27 +718,14 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
     c->prof_steps += steps;
     if ((e = cudaEventRecord(e0, s)) != cudaSuccess) return e;
   }
-  if (temporal) {
-    // the whole interval on chip: P_0 from the reseed output, S_T where the
-    // streaming sequence would leave it
-    const int dst = (steps % 2 == 1) ? sbuf : 1 - sbuf;
-    for (int r = 0; r < c->nruns; r++) {
-      const RunDev &R = c->runs_h[r];
-      TemporalArgs ta{c->runs_h[r], r, steps, (const float *)c->pop[1 - sbuf], (float *)c->pop[dst],
-                      (float *)c->d.terms, c->d.term_slab, c->d.err, c->d_maps};
-      if ((e = launch_temporal(ta, c->temporal_cs, c->temporal_variant, R.nclones, R.W, R.H, s)) != cudaSuccess)
-        return e;
-    }
-  } else {
-    for (int t = 0; t < steps; t++) {
-      StepArgs a{c->d.runs, c->nruns, t, c->pop[cur], c->pop[1 - cur], c->d.terms, c->d.term_slab,
-                 c->d.err, c->total_clones, c->max_nodes,
-                 {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}, c->d_maps};
-      if ((e = launch_step(f64, t == steps - 1, a, c->total_blocks, s, c->step_variant)) != cudaSuccess)
-        return e;
-      cur = 1 - cur;
-    }
-  }
+  // P_0 (the reseed output) is in 1 - sbuf; S_T goes where the streaming
+  // sequence leaves it.  Cluster-resident runs: the whole interval on chip,
+  // one launch each on its own side stream; the streaming runs meanwhile one
+  // step launch per step on the main stream; the side streams join before the
+  // drag reduction (a captured interval holds them as parallel branches).
+  const LbPlan plan = current_plan(c, f64);
+  if ((e = enqueue_lb_steps(c, plan, steps, 1 - sbuf, (steps % 2 == 1) ? sbuf : 1 - sbuf, false)) != cudaSuccess)
+    return e;
   if (prof && (e = cudaEventRecord(e1, s)) != cudaSuccess) return e;
   if ((e = launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, c->any_stress, c->any_momentum, s)) != cudaSuccess) return e;
   if (c->hist_max > 0) {
@@ -834,36 +957,99 @@ extern "C" int clbm_profile_read(clbm_ctx *c, double *step_ms, int *nsteps) {
 // Variant numbering: 0 .. step_variant_count()-1 are the streaming step
 // launches; after them, for cluster sizes 1, 2, 4, 8, 16 (index log2), the
 // cluster-resident interval kernel's thread configurations.
-static void apply_variant(clbm_ctx *c, int v) {
+static int variant_count() { return step_variant_count() + 5 * temporal_variant_count(); }
+
+static void variant_shape(int v, int &cs, int &tv) {
   const int nv = step_variant_count();
-  const int cs0 = c->temporal_cs, sv0 = c->step_variant, tv0 = c->temporal_variant;
-  if (v < nv) {
-    c->step_variant = v;
-    c->temporal_cs = 0;
-  } else {
+  cs = 0;
+  tv = 0;
+  if (v >= nv) {
     const int q = v - nv;
-    c->temporal_cs = 1 << (q / temporal_variant_count());
-    c->temporal_variant = q % temporal_variant_count();
+    cs = 1 << (q / temporal_variant_count());
+    tv = q % temporal_variant_count();
   }
-  // captured intervals hold the previous variant's launches
-  if (c->temporal_cs != cs0 || c->step_variant != sv0 || c->temporal_variant != tv0) destroy_graphs(c);
 }
 
-// Autotuner: time every FP32 step variant on this context's own workload and
-// keep the fastest.  It runs at an interval boundary, reading the current
-// state and writing the idle buffer (overwritten by the next interval's first
-// kernel), so the sampler's state is untouched.  Results are cached per
-// (lattice sizes, clone counts) for the process.
+static int variant_index(int cs, int tv) {
+  return cs ? step_variant_count() + (31 - __builtin_clz((unsigned)cs)) * temporal_variant_count() + tv : 0;
+}
+
+// whether run r's lattice can run cluster-resident at this shape
+static bool shape_fits(const RunDev &R, int cs, int tv) {
+  return R.H >= cs && temporal_max_clusters(cs, tv, R.W, R.H, R.field_mode != 0) >= 1;
+}
+
+// one variant for every run
+static cudaError_t apply_variant(clbm_ctx *c, int v) {
+  int cs, tv;
+  variant_shape(v, cs, tv);
+  return set_plan(c, std::vector<int>(c->nruns, cs), std::vector<int>(c->nruns, tv),
+                  cs ? c->step_variant : v);
+}
+
+// Milliseconds per LB step of a plan on this context's workload, at an
+// interval boundary: timing mode reads the state and writes only the idle
+// buffer, so the sampler is untouched.  One short warm-up pass first.
+static cudaError_t time_plan(clbm_ctx *c, const LbPlan &p, int steps, cudaEvent_t e0, cudaEvent_t e1,
+                             double *ms_per_step) {
+  cudaError_t e = enqueue_lb_steps(c, p, 1, c->s_buf, 1 - c->s_buf, true);
+  if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+  if (e == cudaSuccess) e = enqueue_lb_steps(c, p, steps, c->s_buf, 1 - c->s_buf, true);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  *ms_per_step = ms / steps;
+  return e;
+}
+
+// A plan over every run with the streaming runs (cs == 0) in their own table.
+static cudaError_t full_plan(clbm_ctx *c, const std::vector<int> &cs, const std::vector<int> &tv, int sv,
+                             LbPlan &p) {
+  p = LbPlan{};
+  p.cs = cs;
+  p.tv = tv;
+  p.variant = sv;
+  std::vector<int> streaming;
+  for (int r = 0; r < c->nruns; r++)
+    if (!cs[r]) streaming.push_back(r);
+  if ((int)streaming.size() == c->nruns) {
+    p.table = c->d.runs;
+    p.nstream = c->nruns;
+    for (int q = 0; q < 3; q++) p.tiles[q] = c->total_tiles[q];
+    return cudaSuccess;
+  }
+  cudaError_t e = upload_stream_table(c, streaming);
+  p.table = c->d_runs_stream;
+  p.nstream = c->stream_nruns;
+  for (int q = 0; q < 3; q++) p.tiles[q] = c->stream_tiles[q];
+  return e;
+}
+
+// Autotuner: time the candidates on this context's own workload and keep the
+// fastest.  Uniform candidates first (every run on one variant: the 8
+// streaming launch shapes, then each cluster-resident shape that fits every
+// lattice).  With several runs, each run's own best is then found alone
+// (the best streaming shape against every cluster-resident shape that fits
+// it), and that per-run plan -- cluster-resident runs concurrent with the
+// streaming ones -- is timed as a whole and kept if it beats the uniform
+// winner.  Results are cached per (lattice sizes, clone counts) for the
+// process.
 #include <map>
 #include <mutex>
+struct TuneResult {
+  int best;
+  std::vector<int> cs, tv;
+  int sv;
+};
 static std::mutex g_tune_mutex;
-static std::map<std::vector<long long>, int> g_tune_cache;
+static std::map<std::vector<long long>, TuneResult> g_tune_cache;
 
 extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_per_variant,
                              int *nvariants) {
   if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
-  const int nv = step_variant_count();
-  if (nvariants) *nvariants = nv + 5 * temporal_variant_count();
+  const int nv = step_variant_count(), ntv = temporal_variant_count();
+  if (nvariants) *nvariants = variant_count();
   if (c->precision != CLBM_FP32) {
     if (best) *best = 0;
     return CLBM_OK;
@@ -878,8 +1064,8 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
-      apply_variant(c, it->second);
-      if (best) *best = it->second;
+      CK(set_plan(c, it->second.cs, it->second.tv, it->second.sv));
+      if (best) *best = it->second.best;
       return CLBM_OK;
     }
   }
@@ -887,78 +1073,115 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  int arg = 0;
-  double best_ms = 1e30;
+  auto bail = [&](cudaError_t e) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return clbm_status_from_cuda(e);
+  };
+  const int R = c->nruns;
+  int arg = 0, best_sv = 0;
+  double best_ms = 1e30, best_stream_ms = 1e30;
+  // uniform streaming launch shapes (one launch per step)
   for (int v = 0; v < nv; v++) {
-    StepArgs a{c->d.runs, c->nruns, 0, c->pop[c->s_buf], c->pop[1 - c->s_buf], c->d.terms,
-               c->d.term_slab, c->d.err, c->total_clones, c->max_nodes,
-               {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}, c->d_maps};
-    cudaError_t e = launch_step(false, false, a, c->total_blocks, c->stream, v);  // warm-up
-    if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
-    for (int i = 0; i < launches && e == cudaSuccess; i++)
-      e = launch_step(false, false, a, c->total_blocks, c->stream, v);
-    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
-    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-    float ms = 0.f;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-    if (e != cudaSuccess) {
-      cudaEventDestroy(e0);
-      cudaEventDestroy(e1);
-      return clbm_status_from_cuda(e);
-    }
-    const double per = ms / launches;
+    LbPlan p;
+    cudaError_t e = full_plan(c, std::vector<int>(R, 0), std::vector<int>(R, 0), v, p);
+    double per = 0.0;
+    if (e == cudaSuccess) e = time_plan(c, p, launches, e0, e1, &per);
+    if (e != cudaSuccess) return bail(e);
     if (ms_per_variant) ms_per_variant[v] = per;
-    if (per < best_ms) {
-      best_ms = per;
-      arg = v;
+    if (per < best_stream_ms) {
+      best_stream_ms = per;
+      best_sv = v;
     }
   }
-  // cluster-resident candidates, timed per step over a full-length interval
-  // (their HBM load and store are amortised over the steps)
+  best_ms = best_stream_ms;
+  arg = best_sv;
+  std::vector<int> plan_cs(R, 0), plan_tv(R, 0);
+  // uniform cluster-resident shapes, timed per step over a full-length
+  // interval (their HBM load and store are amortised over the steps)
   const int tsteps = std::min(c->max_steps, 100);
-  int t_cs = 0, t_var = 0;
   for (int cs = 1; cs <= 16; cs *= 2) {
-    for (int tv = 0; tv < temporal_variant_count(); tv++) {
-      const int vidx = nv + (31 - __builtin_clz((unsigned)cs)) * temporal_variant_count() + tv;
+    for (int tv = 0; tv < ntv; tv++) {
+      const int vidx = variant_index(cs, tv);
       if (ms_per_variant) ms_per_variant[vidx] = -1.0;
       bool ok = true;
-      for (const RunDev &R : c->runs_h)
-        if (R.H < cs || temporal_max_clusters(cs, tv, R.W, R.H, R.field_mode != 0) < 1) ok = false;
+      for (const RunDev &Rr : c->runs_h) ok = ok && shape_fits(Rr, cs, tv);
       if (!ok) continue;
-      cudaError_t e = cudaEventRecord(e0, c->stream);
-      for (int r = 0; r < c->nruns && e == cudaSuccess; r++) {
-        const RunDev &R = c->runs_h[r];
-        TemporalArgs ta{c->runs_h[r], r, tsteps, (const float *)c->pop[c->s_buf], (float *)c->pop[1 - c->s_buf],
-                        (float *)c->d.terms, c->d.term_slab, c->d.err, c->d_maps};
-        e = launch_temporal(ta, cs, tv, R.nclones, R.W, R.H, c->stream);
-      }
-      if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
-      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-      float ms = 0.f;
-      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      LbPlan p;
+      cudaError_t e = full_plan(c, std::vector<int>(R, cs), std::vector<int>(R, tv), best_sv, p);
+      double per = 0.0;
+      if (e == cudaSuccess) e = time_plan(c, p, tsteps, e0, e1, &per);
       if (e != cudaSuccess) {  // this shape cannot run here: skip it
         cudaGetLastError();
         continue;
       }
-      const double per = ms / tsteps;
       if (ms_per_variant) ms_per_variant[vidx] = per;
       if (per < best_ms) {
         best_ms = per;
-        t_cs = cs;
-        t_var = tv;
         arg = vidx;
+        plan_cs.assign(R, cs);
+        plan_tv.assign(R, tv);
+      }
+    }
+  }
+  // per-run plan
+  if (R > 1) {
+    std::vector<int> pcs(R, 0), ptv(R, 0);
+    bool any = false, mixed = false;
+    for (int r = 0; r < R; r++) {
+      LbPlan p;
+      p.cs.assign(R, 0);
+      p.tv.assign(R, 0);
+      p.active.assign(R, 0);
+      p.active[r] = 1;
+      p.variant = best_sv;
+      cudaError_t e = upload_stream_table(c, std::vector<int>{r});
+      p.table = c->d_runs_stream;
+      p.nstream = 1;
+      for (int q = 0; q < 3; q++) p.tiles[q] = c->stream_tiles[q];
+      double run_best = 0.0;
+      if (e == cudaSuccess) e = time_plan(c, p, tsteps, e0, e1, &run_best);
+      if (e != cudaSuccess) return bail(e);
+      p.nstream = 0;
+      for (int cs = 1; cs <= 16; cs *= 2)
+        for (int tv = 0; tv < ntv; tv++) {
+          if (!shape_fits(c->runs_h[r], cs, tv)) continue;
+          p.cs[r] = cs;
+          p.tv[r] = tv;
+          double per = 0.0;
+          if (time_plan(c, p, tsteps, e0, e1, &per) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+          }
+          if (per < run_best) {
+            run_best = per;
+            pcs[r] = cs;
+            ptv[r] = tv;
+          }
+        }
+      any = any || pcs[r] > 0;
+    }
+    for (int r = 0; r < R; r++) mixed = mixed || pcs[r] != pcs[0] || ptv[r] != ptv[0];
+    if (any && mixed) {
+      LbPlan p;
+      cudaError_t e = full_plan(c, pcs, ptv, best_sv, p);
+      double per = 0.0;
+      if (e == cudaSuccess) e = time_plan(c, p, tsteps, e0, e1, &per);
+      if (e != cudaSuccess) return bail(e);
+      if (per < best_ms) {
+        best_ms = per;
+        arg = CLBM_VARIANT_PER_RUN;
+        plan_cs = pcs;
+        plan_tv = ptv;
       }
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  c->temporal_cs = t_cs;
-  c->temporal_variant = t_var;
-  if (!t_cs) c->step_variant = arg;
-  destroy_graphs(c);
+  CK(set_plan(c, plan_cs, plan_tv, best_sv));
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
-    g_tune_cache[key] = arg;
+    g_tune_cache[key] = TuneResult{arg, plan_cs, plan_tv, best_sv};
   }
   if (best) *best = arg;
   return CLBM_OK;
@@ -966,18 +1189,43 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
 
 extern "C" int clbm_set_step_variant(clbm_ctx *c, int variant) {
   if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
-  if (variant < 0 || variant >= step_variant_count() + 5 * temporal_variant_count())
-    return fail(CLBM_ERR_INVALID, "no such variant");
+  if (variant < 0 || variant >= variant_count()) return fail(CLBM_ERR_INVALID, "no such variant");
   if (variant >= step_variant_count()) {
     if (c->precision != CLBM_FP32) return fail(CLBM_ERR_INVALID, "cluster-resident intervals are FP32 only");
-    const int q = variant - step_variant_count();
-    const int cs = 1 << (q / temporal_variant_count()), tv = q % temporal_variant_count();
+    int cs, tv;
+    variant_shape(variant, cs, tv);
     for (const RunDev &R : c->runs_h)
-      if (R.H < cs || temporal_max_clusters(cs, tv, R.W, R.H, R.field_mode != 0) < 1)
-        return fail(CLBM_ERR_INVALID, "cluster shape does not fit this workload");
+      if (!shape_fits(R, cs, tv)) return fail(CLBM_ERR_INVALID, "cluster shape does not fit this workload");
   }
-  apply_variant(c, variant);
-  destroy_graphs(c);
+  CK(apply_variant(c, variant));
+  return CLBM_OK;
+}
+
+extern "C" int clbm_set_run_variants(clbm_ctx *c, const int *variants) {
+  if (!c || !variants) return fail(CLBM_ERR_INVALID, "NULL argument");
+  std::vector<int> cs(c->nruns), tv(c->nruns);
+  int sv = -1;
+  for (int r = 0; r < c->nruns; r++) {
+    const int v = variants[r];
+    if (v < 0 || v >= variant_count()) return fail(CLBM_ERR_INVALID, "no such variant");
+    variant_shape(v, cs[r], tv[r]);
+    if (!cs[r]) {
+      if (sv >= 0 && sv != v) return fail(CLBM_ERR_INVALID, "the streaming runs must share one streaming variant");
+      sv = v;
+    } else {
+      if (c->precision != CLBM_FP32) return fail(CLBM_ERR_INVALID, "cluster-resident intervals are FP32 only");
+      if (!shape_fits(c->runs_h[r], cs[r], tv[r]))
+        return fail(CLBM_ERR_INVALID, "cluster shape does not fit this run's lattice");
+    }
+  }
+  CK(set_plan(c, cs, tv, sv >= 0 ? sv : c->step_variant));
+  return CLBM_OK;
+}
+
+extern "C" int clbm_get_run_variants(clbm_ctx *c, int *variants) {
+  if (!c || !variants) return fail(CLBM_ERR_INVALID, "NULL argument");
+  for (int r = 0; r < c->nruns; r++)
+    variants[r] = c->run_cs[r] ? variant_index(c->run_cs[r], c->run_tv[r]) : c->step_variant;
   return CLBM_OK;
 }
 

@@ -274,14 +274,29 @@ int clbm_profile_read(clbm_ctx *ctx, double *step_ms, int *nsteps);
  * step), then the cluster-resident interval kernel (every clone's populations
  * in the shared memory of one thread-block cluster for all the steps of an
  * interval, one launch per interval) for cluster sizes 1, 2, 4, 8, 16 and
- * three thread counts (1024, 512, 256), where the lattice fits.  At most
- * 8 + 15 variants.  *best = chosen candidate,
- * ms_per_variant (nullable, *nvariants entries, -1 = not runnable here) =
- * milliseconds per step.  With ms_per_variant NULL a result cached for the same
- * lattices and clone counts is reused.  FP64 contexts have one variant. */
+ * three thread counts (1024, 512, 256), where every lattice fits: at most
+ * 8 + 15 uniform variants.  With several runs it then times each run alone on
+ * every shape that fits its lattice and, when the runs' own bests differ,
+ * the per-run plan as a whole: each cluster-resident run is one launch per
+ * interval on its own stream, concurrent with one step launch per step of
+ * the streaming runs (a CUDA-graph interval holds them as parallel
+ * branches).  *best = the chosen uniform variant, or CLBM_VARIANT_PER_RUN for
+ * a per-run plan (clbm_get_run_variants); ms_per_variant (nullable,
+ * *nvariants entries, -1 = not runnable here) = milliseconds per step of the
+ * uniform variants.  With ms_per_variant NULL a result cached for the same
+ * lattices and clone counts is reused.  FP64 contexts have one variant.
+ * Every variant and plan gives bit-identical results. */
+#define CLBM_VARIANT_PER_RUN (-1)
 int clbm_autotune(clbm_ctx *ctx, int launches, int *best,
                   double *ms_per_variant, int *nvariants);
+/* one variant (autotuner numbering) for every run */
 int clbm_set_step_variant(clbm_ctx *ctx, int variant);
+/* a variant per run (nruns entries): runs given a cluster-resident variant run
+ * it concurrently, each on its own stream; the runs given a streaming variant
+ * share one step launch per step and must name the same streaming variant */
+int clbm_set_run_variants(clbm_ctx *ctx, const int *variants);
+/* the variant each run uses now (nruns entries) */
+int clbm_get_run_variants(clbm_ctx *ctx, int *variants);
 
 /* Macroscopic fields of a clone's current pre-collision state, HOST arrays of
  * Dx*Dy values in the reference's node order y + Dy*x: rho, ux (shifted by
