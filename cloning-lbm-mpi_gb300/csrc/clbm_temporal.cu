@@ -293,6 +293,9 @@ __device__ __forceinline__ void update_fast(const RunDev &R, float *C, float *U,
 
 // Whether the whole warp's 32-node segment is away from walls, the square and
 // band edges, so all neighbours are in this CTA and nothing bounces back.
+// (Segment classes: 2 = general path, 1 = bulk with the periodic wrap or the
+// band's partial last segment, 0 = interior bulk: every lane a valid node
+// with 0 < x < W-1, so its neighbours sit at constant offsets from it.)
 __device__ __forceinline__ bool segment_is_bulk(bool pad, const RunDev &R, const Band &b, int x, int ly) {
   const int y = b.row0 + ly;
   const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
@@ -305,11 +308,48 @@ __device__ __forceinline__ float field_eps(const TemporalArgs &a, int t) {
   return t + 1 < a.rd.field_steps ? a.rd.f_field_eps : 0.0f;
 }
 
-// Shared memory of one CTA: the band's populations, then (generic kernel)
-// the segment list and one class byte per 32-node segment.
+// Shared memory of one CTA: the band's populations, then the segment list,
+// one class byte per 32-node segment and the two range ends of the list.
 __host__ __device__ inline size_t temporal_smem(int nb) {
   const int nseg = (nb + 31) / 32;
   return sizeof(float) * 9 * (size_t)nb + 2 * (size_t)((nseg + 7) & ~7) + (size_t)((nseg + 15) & ~15) + 16;
+}
+
+// One step of every segment of the band (all but the interval's last step).
+// General segments (walls, band edges, the square's box) come first in the
+// list, then the bulk segments that contain the periodic wrap, then the
+// interior bulk segments, whose nine source and target slots are constant
+// offsets from the node's own (-9 / +9 floats for x -+ 1, -+ rowstep for
+// y -+ 1): no per-node column arithmetic.  Entry k of the list belongs to
+// warp k % NW in every range.
+template <int NW, bool GATHER, bool FIELD>
+__device__ __forceinline__ void band_step(const TemporalArgs &a, const Band &b, float *A,
+                                          const unsigned short *list, int nseg, int ngen, int nwrap,
+                                          int warp, int lane, int t, const float *map, bool &bad) {
+  const RunDev &R = a.rd;
+  const float feps = FIELD ? field_eps(a, t) : 0.0f;
+  float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
+  for (int k = warp; k < ngen; k += NW) {
+    const int i = list[k] * 32 + lane;
+    if (i >= b.nb) continue;
+    if (GATHER)
+      update_general_gather(a, b, i, t, bad, terms);
+    else
+      update_general_local(a, b, A, i, t, bad, terms);
+  }
+  for (int k = ngen + ((warp - ngen) & (NW - 1)); k < nwrap; k += NW) {
+    const int i = list[k] * 32 + lane;
+    if (i >= b.nb) continue;
+    const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
+    const int o0 = x * 9, om = (x == 0 ? b.W - 1 : x - 1) * 9, op = (x == b.W - 1 ? 0 : x + 1) * 9;
+    float *C = A + ly * b.rowstep;
+    update_fast<GATHER, FIELD>(R, C, C - b.rowstep, C + b.rowstep, om, o0, op, map + i, feps, bad);
+  }
+  for (int k = nwrap + ((warp - nwrap) & (NW - 1)); k < nseg; k += NW) {
+    const int i = list[k] * 32 + lane;
+    float *C = A + i * 9;
+    update_fast<GATHER, FIELD>(R, C, C - b.rowstep, C + b.rowstep, -9, 0, 9, map + i, feps, bad);
+  }
 }
 
 // Generic kernel: any W.  The band's nodes form 32-node segments; segments
@@ -335,57 +375,42 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
   load_band<THREADS>(b, A);
   const int nseg = (b.nb + 31) / 32;
   unsigned short *list = (unsigned short *)(A + (size_t)9 * b.nb);
-  unsigned char *general = (unsigned char *)(list + ((nseg + 7) & ~7));
-  int *ngen_s = (int *)(general + ((nseg + 15) & ~15));
+  unsigned char *cls = (unsigned char *)(list + ((nseg + 7) & ~7));
+  int *count_s = (int *)(cls + ((nseg + 15) & ~15));
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   for (int sg = warp; sg < nseg; sg += NW) {
     const int i = sg * 32 + lane;
     const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
-    const bool bulk = segment_is_bulk(i >= b.nb, R, b, x, ly);
-    if (lane == 0) general[sg] = bulk ? 0 : 1;
+    const bool pad = i >= b.nb;
+    const bool bulk = segment_is_bulk(pad, R, b, x, ly);
+    const bool inner = __all_sync(0xffffffffu, !pad && x > 0 && x < b.W - 1);
+    if (lane == 0) cls[sg] = bulk ? (inner ? 0 : 1) : 2;
   }
   __syncthreads();
-  if (warp == 0) {  // the list: general segments, then bulk ones
+  if (warp == 0) {  // the list: general segments, then wrap bulk, then interior bulk
     const unsigned lower = (1u << lane) - 1u;
     int n = 0;
-    for (int pass = 1; pass >= 0; pass--)
+    for (int pass = 2; pass >= 0; pass--) {
       for (int c = 0; c < nseg; c += 32) {
-        const bool take = c + lane < nseg && general[c + lane] == pass;
+        const bool take = c + lane < nseg && cls[c + lane] == pass;
         const unsigned m = __ballot_sync(0xffffffffu, take);
         if (take) list[n + __popc(m & lower)] = (unsigned short)(c + lane);
         n += __popc(m);
-        if (pass == 1 && lane == 0 && c + 32 >= nseg) *ngen_s = n;
       }
+      if (lane == 0 && pass > 0) count_s[2 - pass] = n;
+    }
   }
   __syncthreads();
-  const int ngen = *ngen_s;
+  const int ngen = count_s[0], nwrap = count_s[1];
   const float *map = FIELD ? a.maps + R.map_base + (long long)b.clone * R.nodes + (long long)b.row0 * b.W : nullptr;
   bool bad = false;
   cluster.sync();
-  // every step but the last: bulk segments through update_fast (GATHER known
-  // at compile time), the rest through update_general
+  // every step but the last
   for (int t = 0; t + 1 < a.steps; t++) {
-    const bool gather = (t & 1) == 0;
-    const float feps = FIELD ? field_eps(a, t) : 0.0f;
-    float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
-    for (int k = warp; k < nseg; k += NW) {
-      const int i = list[k] * 32 + lane;
-      if (i >= b.nb) continue;
-      if (k < ngen) {
-        if (gather)
-          update_general_gather(a, b, i, t, bad, terms);
-        else
-          update_general_local(a, b, A, i, t, bad, terms);
-        continue;
-      }
-      const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
-      const int o0 = x * 9, om = (x == 0 ? b.W - 1 : x - 1) * 9, op = (x == b.W - 1 ? 0 : x + 1) * 9;
-      float *C = A + ly * b.rowstep;
-      if (gather)
-        update_fast<true, FIELD>(R, C, C - b.rowstep, C + b.rowstep, om, o0, op, map + i, feps, bad);
-      else
-        update_fast<false, FIELD>(R, C, C - b.rowstep, C + b.rowstep, om, o0, op, map + i, feps, bad);
-    }
+    if ((t & 1) == 0)
+      band_step<NW, true, FIELD>(a, b, A, list, nseg, ngen, nwrap, warp, lane, t, map, bad);
+    else
+      band_step<NW, false, FIELD>(a, b, A, list, nseg, ngen, nwrap, warp, lane, t, map, bad);
     cluster.sync();
   }
   // the last step stores S_T (one step in T: every node through update_general)
