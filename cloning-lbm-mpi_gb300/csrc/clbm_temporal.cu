@@ -134,15 +134,18 @@ __device__ __forceinline__ void update_general(const TemporalArgs &a, const Band
 // opp k) came from -- the pull rules make the two the same slot (own slot opp
 // k when that slot bounces, else (n + c_k, k)) -- unless the target row lies
 // outside the channel or the target inside the square (the push is dropped,
-// as in update_general).
+// as in update_general).  PLAIN: a node off the walls and the square's box
+// (a band-edge row): nothing bounces back and no push is dropped, only the
+// neighbour rows may lie in the adjacent CTAs.
+template <bool PLAIN = false>
 __device__ __forceinline__ void update_general_gather(const TemporalArgs &a, const Band &b, int i, int t,
                                                       bool &bad, float *terms) {
   const RunDev &R = a.rd;
   const int W = b.W, H = b.H, rows = b.rows, rs = b.rowstep;
   const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = b.row0 + ly;
   const int xm = x == 0 ? W - 1 : x - 1, xp = x == W - 1 ? 0 : x + 1;
-  const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
-  const int mask = (in_box || y == 0 || y == H - 1) ? bounce_mask(R, x, y) : 0;
+  const bool in_box = !PLAIN && x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+  const int mask = (!PLAIN && (in_box || y == 0 || y == H - 1)) ? bounce_mask(R, x, y) : 0;
   if (mask & 512) return;  // inside the square
   // byte addresses of column 0 of the rows y-1, y, y+1
   const unsigned rowC = b.own_c + 4u * (unsigned)(ly * rs);
@@ -174,7 +177,7 @@ __device__ __forceinline__ void update_general_gather(const TemporalArgs &a, con
 #pragma unroll
   for (int k = 0; k < 9; k++) {
     const int ok = opp_of(k);
-    if (!((mask >> ok) & 1)) {
+    if (!PLAIN && !((mask >> ok) & 1)) {
       const int cx = cx_of(k), cy = cy_of(k);
       const int tx = cx == 1 ? xp : (cx == -1 ? xm : x);
       const int ty = y + cy;
@@ -291,44 +294,36 @@ __device__ __forceinline__ void update_fast(const RunDev &R, float *C, float *U,
   }
 }
 
-// Whether the whole warp's 32-node segment is away from walls, the square and
-// band edges, so all neighbours are in this CTA and nothing bounces back.
-// (Segment classes: 2 = general path, 1 = bulk with the periodic wrap or the
-// band's partial last segment, 0 = interior bulk: every lane a valid node
-// with 0 < x < W-1, so its neighbours sit at constant offsets from it.)
-__device__ __forceinline__ bool segment_is_bulk(bool pad, const RunDev &R, const Band &b, int x, int ly) {
-  const int y = b.row0 + ly;
-  const bool in_box = x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
-  const bool wall = y == 0 || y == b.H - 1;
-  const bool edge = b.cs > 1 && (ly == 0 || ly == b.rows - 1);
-  return __all_sync(0xffffffffu, pad || !(in_box || wall || edge));
-}
-
 __device__ __forceinline__ float field_eps(const TemporalArgs &a, int t) {
   return t + 1 < a.rd.field_steps ? a.rd.f_field_eps : 0.0f;
 }
 
 // Shared memory of one CTA: the band's populations, then the segment list,
-// one class byte per 32-node segment and the two range ends of the list.
+// one class byte per 32-node segment and the three range ends of the list.
 __host__ __device__ inline size_t temporal_smem(int nb) {
   const int nseg = (nb + 31) / 32;
   return sizeof(float) * 9 * (size_t)nb + 2 * (size_t)((nseg + 7) & ~7) + (size_t)((nseg + 15) & ~15) + 16;
 }
 
 // One step of every segment of the band (all but the interval's last step).
-// General segments (walls, band edges, the square's box) come first in the
-// list, then the bulk segments that contain the periodic wrap, then the
-// interior bulk segments, whose nine source and target slots are constant
-// offsets from the node's own (-9 / +9 floats for x -+ 1, -+ rowstep for
-// y -+ 1): no per-node column arithmetic.  Entry k of the list belongs to
-// warp k % NW in every range.
+// The list holds the segments by class: the square's box and the walls (and
+// a partial last segment) first, then the band-edge rows, the bulk segments
+// with the periodic wrap and the interior bulk segments; entry k belongs to
+// warp k % NW in every range.  Gather step: the first range through the
+// general path, band-edge rows through its plain form (no bounce-back, the
+// neighbour rows through distributed shared memory), wrap segments with
+// per-node column offsets, interior segments with their nine slots at
+// constant offsets from the node's own (-9 / +9 floats for x -+ 1, -+ rowstep
+// for y -+ 1).  Local step: a node touches only its own nine slots, so only
+// the first range (the box: drag terms, the interior) needs the general path.
 template <int NW, bool GATHER, bool FIELD>
 __device__ __forceinline__ void band_step(const TemporalArgs &a, const Band &b, float *A,
-                                          const unsigned short *list, int nseg, int ngen, int nwrap,
+                                          const unsigned short *list, int nseg, const int *range,
                                           int warp, int lane, int t, const float *map, bool &bad) {
   const RunDev &R = a.rd;
   const float feps = FIELD ? field_eps(a, t) : 0.0f;
   float *terms = a.terms + (long long)t * a.term_slab + R.term_base;
+  const int ngen = range[0];
   for (int k = warp; k < ngen; k += NW) {
     const int i = list[k] * 32 + lane;
     if (i >= b.nb) continue;
@@ -337,18 +332,28 @@ __device__ __forceinline__ void band_step(const TemporalArgs &a, const Band &b, 
     else
       update_general_local(a, b, A, i, t, bad, terms);
   }
-  for (int k = ngen + ((warp - ngen) & (NW - 1)); k < nwrap; k += NW) {
+  if (!GATHER) {
+    for (int k = ngen + ((warp - ngen) & (NW - 1)); k < nseg; k += NW) {
+      const int i = list[k] * 32 + lane;
+      float *C = A + i * 9;
+      update_fast<false, FIELD>(R, C, C, C, 0, 0, 0, map + i, feps, bad);
+    }
+    return;
+  }
+  const int nedge = range[1], nwrap = range[2];
+  for (int k = ngen + ((warp - ngen) & (NW - 1)); k < nedge; k += NW)
+    update_general_gather<true>(a, b, list[k] * 32 + lane, t, bad, terms);
+  for (int k = nedge + ((warp - nedge) & (NW - 1)); k < nwrap; k += NW) {
     const int i = list[k] * 32 + lane;
-    if (i >= b.nb) continue;
     const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
     const int o0 = x * 9, om = (x == 0 ? b.W - 1 : x - 1) * 9, op = (x == b.W - 1 ? 0 : x + 1) * 9;
     float *C = A + ly * b.rowstep;
-    update_fast<GATHER, FIELD>(R, C, C - b.rowstep, C + b.rowstep, om, o0, op, map + i, feps, bad);
+    update_fast<true, FIELD>(R, C, C - b.rowstep, C + b.rowstep, om, o0, op, map + i, feps, bad);
   }
   for (int k = nwrap + ((warp - nwrap) & (NW - 1)); k < nseg; k += NW) {
     const int i = list[k] * 32 + lane;
     float *C = A + i * 9;
-    update_fast<GATHER, FIELD>(R, C, C - b.rowstep, C + b.rowstep, -9, 0, 9, map + i, feps, bad);
+    update_fast<true, FIELD>(R, C, C - b.rowstep, C + b.rowstep, -9, 0, 9, map + i, feps, bad);
   }
 }
 
@@ -378,39 +383,46 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
   unsigned char *cls = (unsigned char *)(list + ((nseg + 7) & ~7));
   int *count_s = (int *)(cls + ((nseg + 15) & ~15));
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  // segment classes: 4 touches the square's box, 3 a wall row or past the
+  // band's end (partial last segment), 2 a band-edge row (neighbour row in
+  // another CTA), 1 bulk with the periodic wrap, 0 interior bulk
   for (int sg = warp; sg < nseg; sg += NW) {
     const int i = sg * 32 + lane;
-    const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
+    const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W, y = b.row0 + ly;
     const bool pad = i >= b.nb;
-    const bool bulk = segment_is_bulk(pad, R, b, x, ly);
+    const bool box = !pad && x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
+    const bool wall = pad || y == 0 || y == b.H - 1;
+    const bool edge = !pad && b.cs > 1 && (ly == 0 || ly == b.rows - 1);
     const bool inner = __all_sync(0xffffffffu, !pad && x > 0 && x < b.W - 1);
-    if (lane == 0) cls[sg] = bulk ? (inner ? 0 : 1) : 2;
+    const int c = __any_sync(0xffffffffu, box) ? 4 : __any_sync(0xffffffffu, wall) ? 3
+                  : __any_sync(0xffffffffu, edge) ? 2 : inner ? 0 : 1;
+    if (lane == 0) cls[sg] = (unsigned char)c;
   }
   __syncthreads();
-  if (warp == 0) {  // the list: general segments, then wrap bulk, then interior bulk
+  if (warp == 0) {  // the list, class 4 first; range ends after classes 3, 2, 1
     const unsigned lower = (1u << lane) - 1u;
     int n = 0;
-    for (int pass = 2; pass >= 0; pass--) {
+    for (int pass = 4; pass >= 0; pass--) {
       for (int c = 0; c < nseg; c += 32) {
         const bool take = c + lane < nseg && cls[c + lane] == pass;
         const unsigned m = __ballot_sync(0xffffffffu, take);
         if (take) list[n + __popc(m & lower)] = (unsigned short)(c + lane);
         n += __popc(m);
       }
-      if (lane == 0 && pass > 0) count_s[2 - pass] = n;
+      if (lane == 0 && pass >= 1 && pass <= 3) count_s[3 - pass] = n;
     }
   }
   __syncthreads();
-  const int ngen = count_s[0], nwrap = count_s[1];
+  const int range[3] = {count_s[0], count_s[1], count_s[2]};
   const float *map = FIELD ? a.maps + R.map_base + (long long)b.clone * R.nodes + (long long)b.row0 * b.W : nullptr;
   bool bad = false;
   cluster.sync();
   // every step but the last
   for (int t = 0; t + 1 < a.steps; t++) {
     if ((t & 1) == 0)
-      band_step<NW, true, FIELD>(a, b, A, list, nseg, ngen, nwrap, warp, lane, t, map, bad);
+      band_step<NW, true, FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
     else
-      band_step<NW, false, FIELD>(a, b, A, list, nseg, ngen, nwrap, warp, lane, t, map, bad);
+      band_step<NW, false, FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
     cluster.sync();
   }
   // the last step stores S_T (one step in T: every node through update_general)
