@@ -283,6 +283,7 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
     }
     R.f_beta = (float)d.beta;
     R.f_force = f32_force(R.f_beta, R.f_cforce);
+    R.f_pairs = f32_pairs(R.f_omega, R.f_om1, R.f_c13, R.f_c2, R.f_force);
     R.perturb_mode = d.perturb_mode;
     R.resample_mode = d.resample_mode;
     R.drag_mode = d.drag_mode;

@@ -3,6 +3,7 @@
 // classification) and the counter-based / emulated random streams.
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace clbm {
@@ -58,6 +59,40 @@ __host__ __device__ inline F32Force f32_force(float beta, float cforce) {
   return f;
 }
 
+// Two FP32 values in one 64-bit word, the operand of the packed (f32x2)
+// arithmetic: lane 0 in the low half, lane 1 in the high half.
+typedef unsigned long long f2_t;
+__host__ __device__ inline f2_t f2_bits(float lo, float hi) {
+  unsigned l, h;
+  memcpy(&l, &lo, 4);
+  memcpy(&h, &hi, 4);
+  return ((f2_t)h << 32) | l;
+}
+
+// Constant operands of the packed FP32 collision (collide_f32_pairs): lane 0
+// serves the pairs (1,3) / (5,7), lane 1 the pairs (2,4) / (6,8).
+struct F32Pairs {
+  f2_t om1, omega, w9, w36, c13, c2;  // (v, v)
+  f2_t fb9_0, fb9_m, f13_0, f2_m;     // (fb9, 0), (fb9, -fb9), (f13, -0), (f2, -f2)
+};
+__host__ __device__ inline void f32_pairs_force(F32Pairs &p, const F32Force &f) {
+  p.fb9_0 = f2_bits(f.fb9, 0.0f);
+  p.fb9_m = f2_bits(f.fb9, -f.fb9);
+  p.f13_0 = f2_bits(f.f13, -0.0f);
+  p.f2_m = f2_bits(f.f2, -f.f2);
+}
+__host__ __device__ inline F32Pairs f32_pairs(float omega, float om1, float c13, float c2, const F32Force &f) {
+  F32Pairs p;
+  p.om1 = f2_bits(om1, om1);
+  p.omega = f2_bits(omega, omega);
+  p.w9 = f2_bits(1.0f / 9.0f, 1.0f / 9.0f);
+  p.w36 = f2_bits(1.0f / 36.0f, 1.0f / 36.0f);
+  p.c13 = f2_bits(c13, c13);
+  p.c2 = f2_bits(c2, c2);
+  f32_pairs_force(p, f);
+  return p;
+}
+
 // One independent run (lattice, square, physics, clone block) of a batch.
 struct RunDev {
   int W, H;                    // Dx, Dy
@@ -88,6 +123,7 @@ struct RunDev {
   // cforce = 1 - omega'/2 exactly; f_force = f32_force(f_beta, f_cforce)
   float f_omega, f_om1, f_c13, f_c2, f_cforce, f_beta;
   F32Force f_force;
+  F32Pairs f_pairs;            // the same constants packed for the f32x2 collision
   int perturb_mode, resample_mode, ranks, nsnap;
   unsigned long long seed;
   unsigned run_id;

@@ -130,6 +130,43 @@ __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b);
 __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 }  // namespace f32op
 
+// Packed FP32 arithmetic (Blackwell f32x2): each lane is the IEEE
+// round-to-nearest operation of its scalar counterpart, so a packed
+// expression gives the same bits as the two scalar ones it replaces.
+namespace f32x2op {
+__device__ __forceinline__ float lo(f2_t v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float hi(f2_t v) { return __uint_as_float((unsigned)(v >> 32)); }
+__device__ __forceinline__ f2_t add(f2_t a, f2_t b) {
+  f2_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t sub(f2_t a, f2_t b) {
+  f2_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t mul(f2_t a, f2_t b) {
+  f2_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t fma(f2_t a, f2_t b, f2_t c) {
+  f2_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+}  // namespace f32x2op
+
+// 1/x by the hardware reciprocal approximation (the value x / y takes in
+// fast approximate division for x = 1, without its range fix-ups: x here is
+// a density near 1)
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // The collision organised by opposite pairs (k, opp k): they share |c.u|, so
 // with e = c_k.u the equilibria split into an even part
 // w (drho + rho (4.5 e^2 - 1.5 u^2)) and an odd part +-3 w rho e, and the
@@ -157,20 +194,32 @@ __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_
 // Every operation is an explicitly rounded intrinsic (the fused
 // multiply-adds chosen here, none left to the compiler), so the result is the
 // same bit for bit in every kernel that inlines it.
+//
+// The four direction pairs are evaluated two at a time in packed f32x2
+// arithmetic: the axis pairs (1,3) and (2,4) in lanes 0 and 1 with e = (ux,
+// uy), the diagonal pairs (5,7) and (6,8) with e = (ux + uy, uy - ux).  Lane
+// 1 of the axis Guo term is fma(0, uy, fx) = fx and its odd part
+// fma(c13, ty, -0) = c13 ty, so every lane is the scalar expression of its
+// pair; the k -> (k, opp k) sums and differences of the moments are packed
+// the same way.  k holds the run's constants in lane pairs (F32Pairs).
 __device__ __forceinline__ float collide_f32_pairs(const float g[9], float out[9], float omega,
-                                                   float om1, float c13, float c2,
-                                                   const F32Force &f) {
+                                                   const F32Force &f, const F32Pairs &k) {
   using namespace f32op;
-  const float a57 = add(g[5], g[7]), a68 = add(g[6], g[8]);
-  const float s57 = sub(g[5], g[7]);
-  const float drho = add(add(add(g[0], add(g[1], g[3])), add(g[2], g[4])), add(a57, a68));
-  const float jx = add(sub(g[1], g[3]), add(s57, sub(g[8], g[6])));
-  const float jy = add(sub(g[2], g[4]), add(s57, sub(g[6], g[8])));
+  namespace X = f32x2op;
+  const f2_t g12 = f2_bits(g[1], g[2]), g34 = f2_bits(g[3], g[4]);
+  const f2_t g56 = f2_bits(g[5], g[6]), g78 = f2_bits(g[7], g[8]);
+  const f2_t a1324 = X::add(g12, g34), d1324 = X::sub(g12, g34);  // (g1 +- g3, g2 +- g4)
+  const f2_t a5768 = X::add(g56, g78);                            // (g5 + g7, g6 + g8)
+  const float s57 = sub(g[5], g[7]), t86 = sub(g[8], g[6]);
+  const float drho = add(add(add(g[0], X::lo(a1324)), X::hi(a1324)), add(X::lo(a5768), X::hi(a5768)));
+  // jy's s57 + (g6 - g8) is s57 - t86: the rounded g6 - g8 is exactly -t86
+  const float jx = add(X::lo(d1324), add(s57, t86));
+  const float jy = add(X::hi(d1324), sub(s57, t86));
   const float rho = add(1.0f, drho);
   // 1/(1 + drho): the hardware approximation r0 of 1/rho refined by one
   // Newton-Raphson step on the unrounded density, r0 + r0 ((1 - r0) - drho r0)
   // (1 - r0 is exact: r0 is near 1)
-  const float r0 = __fdividef(1.0f, rho);
+  const float r0 = rcp_approx(rho);
   const float inv = fma(r0, fma(-drho, r0, sub(1.0f, r0)), r0);
   const float ux = fma(jx, inv, mul(f.hb, inv));
   const float uy = mul(jy, inv);
@@ -179,37 +228,30 @@ __device__ __forceinline__ float collide_f32_pairs(const float g[9], float out[9
   const float base = fma(-rho, u2, drho);  // even part before the e^2 term (per unit weight)
   const float fx = mul(f.fbm3, ux);         // Guo even part for cx = 0 (per unit weight)
   // k = 0
-  out[0] = fma(om1, g[0], mul(4.0f / 9.0f, fma(omega, base, fx)));
+  out[0] = fma(X::lo(k.om1), g[0], mul(4.0f / 9.0f, fma(omega, base, fx)));
   const float r45 = mul(4.5f, rho);
-  // axis pairs (1,3): e = ux, cx = 1; (2,4): e = uy, cx = 0
+  const f2_t R45 = f2_bits(r45, r45), BASE = f2_bits(base, base), FX = f2_bits(fx, fx);
+  // axis pairs: lane 0 (1,3) e = ux, cx = 1; lane 1 (2,4) e = uy, cx = 0
   {
-    const float w = 1.0f / 9.0f, e = ux;
-    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(f.fb9, e, fx)));
-    const float od = fma(c13, tx, f.f13);
-    out[1] = fma(om1, g[1], add(ev, od));
-    out[3] = fma(om1, g[3], sub(ev, od));
+    const f2_t e = f2_bits(ux, uy), t = f2_bits(tx, ty);
+    const f2_t ev = X::mul(k.w9, X::fma(k.omega, X::fma(X::mul(R45, e), e, BASE), X::fma(k.fb9_0, e, FX)));
+    const f2_t od = X::fma(k.c13, t, k.f13_0);
+    const f2_t o12 = X::fma(k.om1, g12, X::add(ev, od)), o34 = X::fma(k.om1, g34, X::sub(ev, od));
+    out[1] = X::lo(o12);
+    out[2] = X::hi(o12);
+    out[3] = X::lo(o34);
+    out[4] = X::hi(o34);
   }
+  // diagonal pairs: lane 0 (5,7) e = ux + uy, cx = 1; lane 1 (6,8) e = uy - ux, cx = -1
   {
-    const float w = 1.0f / 9.0f, e = uy;
-    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fx));
-    const float od = mul(c13, ty);
-    out[2] = fma(om1, g[2], add(ev, od));
-    out[4] = fma(om1, g[4], sub(ev, od));
-  }
-  // diagonal pairs (5,7): e = ux + uy, cx = 1; (6,8): e = uy - ux, cx = -1
-  {
-    const float w = 1.0f / 36.0f, e = add(ux, uy);
-    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(f.fb9, e, fx)));
-    const float od = fma(c2, add(tx, ty), f.f2);
-    out[5] = fma(om1, g[5], add(ev, od));
-    out[7] = fma(om1, g[7], sub(ev, od));
-  }
-  {
-    const float w = 1.0f / 36.0f, e = sub(uy, ux);
-    const float ev = mul(w, fma(omega, fma(mul(r45, e), e, base), fma(-f.fb9, e, fx)));
-    const float od = fma(c2, sub(ty, tx), -f.f2);
-    out[6] = fma(om1, g[6], add(ev, od));
-    out[8] = fma(om1, g[8], sub(ev, od));
+    const f2_t e = f2_bits(add(ux, uy), sub(uy, ux)), t = f2_bits(add(tx, ty), sub(ty, tx));
+    const f2_t ev = X::mul(k.w36, X::fma(k.omega, X::fma(X::mul(R45, e), e, BASE), X::fma(k.fb9_m, e, FX)));
+    const f2_t od = X::fma(k.c2, t, k.f2_m);
+    const f2_t o56 = X::fma(k.om1, g56, X::add(ev, od)), o78 = X::fma(k.om1, g78, X::sub(ev, od));
+    out[5] = X::lo(o56);
+    out[6] = X::hi(o56);
+    out[7] = X::lo(o78);
+    out[8] = X::hi(o78);
   }
   return drho;
 }
@@ -220,9 +262,11 @@ __device__ __forceinline__ float collide_f32_run(const RunDev &R, const float S[
                                                  const float *field = nullptr, float feps = 0.f) {
   if (field) {
     const F32Force f = f32_force(field_beta_f32(R.f_beta, feps, *field), R.f_cforce);
-    return collide_f32_pairs(S, P, R.f_omega, R.f_om1, R.f_c13, R.f_c2, f);
+    F32Pairs k = R.f_pairs;
+    f32_pairs_force(k, f);
+    return collide_f32_pairs(S, P, R.f_omega, f, k);
   }
-  return collide_f32_pairs(S, P, R.f_omega, R.f_om1, R.f_c13, R.f_c2, R.f_force);
+  return collide_f32_pairs(S, P, R.f_omega, R.f_force, R.f_pairs);
 }
 
 // Drag terms from shifted populations, rest parts removed analytically:
