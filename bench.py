@@ -11,8 +11,10 @@ interval).  One bench "step" is one cloning interval.
   torchrun --nproc-per-node N bench.py --gpus N     (independent replicas)
 
 value      device time (CUDA events on the sampler's stream) of K intervals,
-           state resident in HBM; inputs (2 x 2.4 GB population buffers) are
-           larger than L2, so no flush is needed between intervals.
+           each interval and its cloning step replayed as one CUDA graph
+           (--eager: enqueued launch by launch), state resident in HBM; inputs
+           (2 x 2.4 GB population buffers) are larger than L2, so no flush is
+           needed between intervals.
 e2e        the same metric through the C ABI as a driver calls it: the initial
            populations loaded from pinned host memory in the reference's AoS
            FP64 layout, then per interval the drag series, labels, weights and
@@ -21,7 +23,11 @@ roofline   the dominant kernel (the stream-collide step, or the cluster-resident
            interval kernel when the autotuner picks it): algorithmic bytes
            (72 B/LUP FP32, 144 B/LUP FP64: one read and one write of nine
            populations) per step / its mean duration, from CUDA event pairs
-           around the step (or interval) launches inside the timed region.
+           around the step (or interval) launches of one eagerly enqueued
+           interval after the timed region; for the cluster-resident kernel an
+           HBM-equivalent rate, with its binding resources from its ncu summary.
+fp64_same_workload  the same workload in the FP64 mode (the reference's
+           arithmetic), for the like-for-like ratio to the CPU baseline.
 cpu_baseline the oracle's C port of the reference hot loop on this host's cores.
 """
 from __future__ import annotations
@@ -114,6 +120,37 @@ def ncu_traffic(kernel_file: str):
         return None
     m = re.search(r"traffic_bytes_per_launch_full_size:\s*([0-9.eE+]+)", p.read_text())
     return float(m.group(1)) if m else None
+
+
+def ncu_issue_busy(kernel_file: str):
+    """issue-slot use of a kernel from its ncu summary in profiles/ (fraction)."""
+    p = REPO / "profiles" / kernel_file
+    if not p.exists():
+        return None
+    m = re.search(r"\| issue slots busy \| ([0-9.]+) %", p.read_text())
+    return float(m.group(1)) / 100 if m else None
+
+
+def fp64_same_workload(wl, steps: int = 2):
+    """The same workload in FP64 (the reference's arithmetic, bit-identical to
+    the oracle): clone-LUPS/s over `steps` intervals after one warm-up,
+    CUDA-event timed, state resident."""
+    import torch
+    import clbm
+    s = clbm.Sampler(wl.descs(), clbm.FP64, max_steps=wl.steps, flags=clbm.FLAG_GRAPH)
+    for i, r in enumerate(wl.runs):
+        s.init_equilibrium(i, r.u0, wl.init_noise, r.seed)
+    stream = torch.cuda.ExternalStream(s.stream())
+    s.run_sampler(wl.steps, 1)
+    s.sync()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    s.run_sampler(wl.steps, steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    s.close()
+    return wl.lattice_updates_per_interval * steps / (ms / 1e3)
 
 
 def dist_setup(args):
@@ -357,7 +394,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--graph", action="store_true", help="replay each interval as a CUDA graph")
+    ap.add_argument("--eager", dest="graph", action="store_false",
+                    help="enqueue every interval's launches from the host instead of replaying CUDA graphs")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 run of the same workload")
     ap.add_argument("--variant", type=int, default=None,
                     help="use this interval kernel variant instead of autotuning (profiling)")
     ap.add_argument("--study", choices=["precision", "adjoint", "drag"], default=None)
@@ -474,11 +513,11 @@ def main():
             clbm.check(clbm.lib().clbm_load_run_aos_f64(s.h, i, host[i].data_ptr()), "load")
         h2d = sum(h.numel() * 8 for h in host)
         for _ in range(args.steps):
-            s.run_interval(wl.steps)
+            # one interval and its cloning step (a CUDA graph unless --eager)
+            s.run_sampler(wl.steps, 1)
             for i in range(len(wl.runs)):
                 d = s.drag(i)
                 d2h += d.nbytes
-            s.clone_step()
             for i in range(len(wl.runs)):
                 cr = s.clone_result(i)
                 d2h += cr["labels"].nbytes + cr["weights"].nbytes + 8 + cr["copies_pre"].nbytes * 2
@@ -489,10 +528,13 @@ def main():
                "note": "initial AoS FP64 populations from pinned host memory (amortised over the "
                        "steps) + per-interval drag series, labels, weights, copy numbers, R_t"}
 
+    s.close()
+    fp64 = None
+    if wl.precision == clbm.FP32 and not args.no_fp64 and rank == 0:
+        fp64 = fp64_same_workload(wl)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(wl)
-    s.close()
     if rank != 0:
         return
     clocks = clk.summary()
@@ -519,9 +561,22 @@ def main():
                                  "an interval, so DRAM traffic per launch (traffic, one interval) is "
                                  "a small fraction of the 72 B/LUP a streaming step must move; "
                                  "achieved counts those algorithmic bytes, hence frac > 1 = the gain "
-                                 "over the HBM roofline of streaming; the streaming step kernel's "
-                                 "own figures are under streaming_step",
+                                 "over the HBM roofline of streaming; it is an HBM-equivalent rate, "
+                                 "not HBM utilisation (DRAM is ~1 % busy): the binding resources are "
+                                 "under binding; the streaming step kernel's own figures are under "
+                                 "streaming_step",
+                         "hbm_equivalent": True,
+                         "binding": {"resources": "per-step cluster barrier and instruction issue",
+                                     "issue_slots_busy": ncu_issue_busy(f"{vinfo['kernel']}_{args.workload}.md"),
+                                     "source": f"profiles/{vinfo['kernel']}_{args.workload}.md (ncu)"},
                          "streaming_step": stream_ref} if cluster else {})},
+        "fp64_same_workload": None if fp64 is None else {
+            "value": fp64, "unit": "clone-LUPS/s",
+            "fp32_over_fp64": value / fp64,
+            "vs_cpu_baseline": None if cpu is None else fp64 / cpu["value"],
+            "note": "the same workload in the FP64 mode (reference arithmetic, bit-identical to the "
+                    "oracle), device-timed over 2 intervals: the like-for-like figure against the "
+                    "FP64 CPU baseline"},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches_per_interval * args.steps,
