@@ -458,6 +458,7 @@ def main():
         s.profile(True)
         s.run_sampler(wl.steps, 1)
     step_ms, nsteps = s.profile_read()
+    field_ms, nfield = s.profile_read_fields()
     s.profile(False)
     lups_interval = wl.lattice_updates_per_interval
     value = world * lups_interval * args.steps / (ms / 1e3)
@@ -577,6 +578,10 @@ def main():
             "note": "the same workload in the FP64 mode (reference arithmetic, bit-identical to the "
                     "oracle), device-timed over 2 intervals: the like-for-like figure against the "
                     "FP64 CPU baseline"},
+        **({"field": {"ms_per_interval": field_ms / nfield,
+                      "share_of_interval": (field_ms / nfield) / (ms / args.steps),
+                      "kernels": "k_field_stage1 + k_field_stage2 (CUDA events around them in the "
+                                 "eagerly enqueued intervals)"}} if nfield else {}),
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches_per_interval * args.steps,

@@ -33,7 +33,7 @@ EXPORTS = [
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
-    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_autotune", "clbm_set_step_variant", "clbm_set_run_variants", "clbm_get_run_variants", "clbm_shard_plan", "clbm_ref_random_field",
+    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_profile_read_fields", "clbm_autotune", "clbm_set_step_variant", "clbm_set_run_variants", "clbm_get_run_variants", "clbm_shard_plan", "clbm_ref_random_field",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -112,6 +112,7 @@ def lib() -> C.CDLL:
         L.clbm_set_run_variants.argtypes = [vp, vp]
         L.clbm_get_run_variants.argtypes = [vp, vp]
         L.clbm_profile_read.argtypes = [vp, C.POINTER(d), C.POINTER(i)]
+        L.clbm_profile_read_fields.argtypes = [vp, C.POINTER(d), C.POINTER(i)]
         L.clbm_error_word.argtypes = [vp, C.POINTER(C.c_uint), i]
         L.clbm_sync.argtypes = [vp]
         L.clbm_stream.argtypes = [vp]
@@ -398,6 +399,11 @@ class Sampler:
     def profile_read(self) -> tuple[float, int]:
         ms, n = C.c_double(), C.c_int()
         check(lib().clbm_profile_read(self.h, C.byref(ms), C.byref(n)), "clbm_profile_read")
+        return ms.value, n.value
+
+    def profile_read_fields(self) -> tuple[float, int]:
+        ms, n = C.c_double(), C.c_int()
+        check(lib().clbm_profile_read_fields(self.h, C.byref(ms), C.byref(n)), "clbm_profile_read_fields")
         return ms.value, n.value
 
     def error_word(self, clear: bool = False) -> int:

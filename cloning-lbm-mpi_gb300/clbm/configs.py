@@ -31,6 +31,10 @@ class Run:
     seed: int
     perturb_mode: int = PERTURB_UNIFORM
     resample_mode: int = RESAMPLE_REFERENCE
+    # random body-force field of the forcing variant (0 steps: none)
+    field_steps: int = 0
+    field_eps: float = 0.0
+    field_sigma: float = 32.0
 
     @property
     def xmin(self):
@@ -62,7 +66,9 @@ class Run:
                        nclones=self.nclones, ranks=1, tau=self.tau, beta=self.beta,
                        alpha=self.k, force_scale=1.0 / self.F0, force_shift=0.0, dt=self.dt,
                        perturb_mode=self.perturb_mode, resample_mode=self.resample_mode,
-                       eps=self.noise, seed=self.seed, nsnap=0)
+                       eps=self.noise, seed=self.seed, nsnap=0,
+                       field_mode=1 if self.field_steps > 0 else 0, field_steps=self.field_steps,
+                       field_eps=self.field_eps, field_sigma=self.field_sigma)
 
 
 @dataclass
@@ -106,6 +112,25 @@ def c4() -> Workload:
     return Workload("c4_uneven_8x256", runs, 100, 40, FP32)
 
 
+def c3_forcing() -> Workload:
+    """The forcing variant on the 4096-clone 256x64 channel: every clone draws
+    a Gaussian random body-force field (covariance exp(-r^2/(2 sigma^2)),
+    sigma = 32 as in the reference, amplitude eps = 0.1) at the start of each
+    interval and steps its first 20 of the 100 steps under it
+    (src/mpi_LBM_GK_forcing.cpp:333-364)."""
+    return Workload("c3f_4096x256x64_fp32_forcing",
+                    [Run(256, 64, 12, 64, 32, 4096, 0.04, 0.55, 0.3, 1e-5, 3,
+                         field_steps=20, field_eps=0.1, field_sigma=32.0)], 100, 100, FP32)
+
+
+def c3_forcing_small() -> Workload:
+    """256 clones of the forcing workload: the case the ncu captures of the
+    random-field kernels run on."""
+    return Workload("c3fs_256x256x64_fp32_forcing",
+                    [Run(256, 64, 12, 64, 32, 256, 0.04, 0.55, 0.3, 1e-5, 3,
+                         field_steps=20, field_eps=0.1, field_sigma=32.0)], 100, 100, FP32)
+
+
 def c3_small() -> Workload:
     """256 clones of the c3 lattice (151 MB per FP32 buffer, above L2): the
     case the ncu captures of the step kernel run on."""
@@ -131,4 +156,4 @@ def c5() -> Workload:
                     200, 1, FP32)
 
 
-WORKLOADS = {"c5": c5, "c1": c1, "c2": c2, "c2f32": c2_fp32, "c3": c3, "c3s": c3_small, "c3m": c3_medium, "c4": c4}
+WORKLOADS = {"c5": c5, "c1": c1, "c2": c2, "c2f32": c2_fp32, "c3": c3, "c3f": c3_forcing, "c3fs": c3_forcing_small, "c3s": c3_small, "c3m": c3_medium, "c4": c4}

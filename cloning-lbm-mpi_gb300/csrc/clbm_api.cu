@@ -67,6 +67,8 @@ struct clbm_ctx {
   std::vector<cudaEvent_t> ev;  // 2 per profiled interval
   int ev_used = 0;
   int prof_steps = 0;
+  std::vector<cudaEvent_t> fev;  // 2 per profiled interval with random fields
+  int fev_used = 0;
   int max_nodes = 0;
   int total_tiles[3] = {0, 0, 0};
   int step_variant = 0;  // FP32 step launch variant (clbm_autotune)
@@ -86,6 +88,7 @@ struct clbm_ctx {
   bool any_field = false;
   float *d_spec = nullptr, *d_maps = nullptr;
   float2 *d_tw = nullptr, *d_ybuf = nullptr;
+  float *d_fa = nullptr;  // stage-1 DFT operand images of the field runs
   int field_max_w = 0, field_max_m1 = 0, field_max_m2 = 0, field_max_tiles2 = 0;
   std::vector<int> field_negative;  // spectrum entries below -1e-15 (clamped to 0)
   // lineage history (clbm_enable_history)
@@ -171,10 +174,11 @@ extern "C" int clbm_destroy(clbm_ctx *c) {
                   c->d.pert, c->d.partials, c->d.scratch_i, c->d.scratch_d, c->d.snaps,
                   c->d.rvalues, c->d.logr, c->d.err, c->d.terms, c->d_identity, c->d_zeros,
                   c->adj.s0, c->adj.ckpt, c->adj.seg, c->adj.sig[0], c->adj.sig[1],
-                  c->hist_drag, c->hist_labels, c->d_spec, c->d_maps, c->d_tw, c->d_ybuf};
+                  c->hist_drag, c->hist_labels, c->d_spec, c->d_maps, c->d_tw, c->d_ybuf, c->d_fa};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->fev) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return CLBM_OK;
@@ -226,7 +230,8 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
   c->desc.assign(runs, runs + nruns);
   c->snaps_loaded.assign(nruns, 0);
   c->runs_h.resize(nruns);
-  long long pop = 0, terms = 0, snaps = 0, spec = 0, tw = 0, ybuf = 0, maps = 0;
+  long long pop = 0, terms = 0, snaps = 0, spec = 0, tw = 0, ybuf = 0, maps = 0, fa = 0;
+  std::vector<float> h_fa;
   std::vector<float> h_spec;
   std::vector<float2> h_tw;
   c->field_negative.assign(nruns, 0);
@@ -323,6 +328,12 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
       R.tw1_base = tw;
       R.tw2_base = tw + M1;
       R.y_base = ybuf;
+      R.f_mpad = field_dft_mpad(d.width);
+      R.f_kchunks = field_dft_kchunks(M1);
+      R.fa_base = fa;
+      h_fa.resize(fa + (size_t)R.f_mpad * 32 * R.f_kchunks);
+      build_field_dft_image(d.width, M1, R.f_mpad, R.f_kchunks, h_fa.data() + fa);
+      fa += (long long)R.f_mpad * 32 * R.f_kchunks;
       R.map_base = maps;
       h_spec.resize(spec + (size_t)M1 * M2);
       for (int a = 0; a < M1; a++)
@@ -406,6 +417,8 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
     if ((e = dalloc(c->d_spec, (size_t)spec)) != cudaSuccess) return bail(e);
     if ((e = dalloc(c->d_tw, (size_t)tw)) != cudaSuccess) return bail(e);
     if ((e = dalloc(c->d_ybuf, (size_t)ybuf)) != cudaSuccess) return bail(e);
+    if ((e = dalloc(c->d_fa, (size_t)fa)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemcpy(c->d_fa, h_fa.data(), sizeof(float) * fa, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e);
     if ((e = dalloc(c->d_maps, (size_t)maps)) != cudaSuccess) return bail(e);
     if ((e = cudaMemcpy(c->d_spec, h_spec.data(), sizeof(float) * spec, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e);
     if ((e = cudaMemcpy(c->d_tw, h_tw.data(), sizeof(float2) * tw, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e);
@@ -696,10 +709,22 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
     if (e != cudaSuccess) return e;
   }
   if (c->any_field) {
-    FieldArgs fa{c->d.runs, c->nruns, c->d.state, c->d_spec, c->d_tw, c->d_ybuf, c->d_maps};
+    if (prof) {  // an event pair around the field kernels
+      while ((size_t)c->fev_used + 2 > c->fev.size()) {
+        cudaEvent_t ne;
+        if ((e = cudaEventCreate(&ne)) != cudaSuccess) return e;
+        c->fev.push_back(ne);
+      }
+      if ((e = cudaEventRecord(c->fev[c->fev_used], s)) != cudaSuccess) return e;
+    }
+    FieldArgs fa{c->d.runs, c->nruns, c->d.state, c->d_spec, c->d_tw, c->d_ybuf, c->d_maps, c->d_fa, c->d.err};
     e = launch_fields(fa, c->total_clones, c->field_max_w, c->field_max_m1, c->field_max_m2,
                       c->field_max_tiles2, s);
     if (e != cudaSuccess) return e;
+    if (prof) {
+      if ((e = cudaEventRecord(c->fev[c->fev_used + 1], s)) != cudaSuccess) return e;
+      c->fev_used += 2;
+    }
   }
   ReseedArgs ra{c->d.runs, c->nruns, S, c->pop[1 - sbuf], c->d.labels, c->d.mark, c->d.pert,
                 c->d.prefactors, c->d.snaps, c->d.state, c->d.err, c->d_maps};
@@ -936,6 +961,7 @@ extern "C" int clbm_profile(clbm_ctx *c, int enable) {
   c->profiling = enable != 0;
   c->ev_used = 0;
   c->prof_steps = 0;
+  c->fev_used = 0;
   return CLBM_OK;
 }
 
@@ -952,6 +978,21 @@ extern "C" int clbm_profile_read(clbm_ctx *c, double *step_ms, int *nsteps) {
   *nsteps = c->prof_steps;
   c->ev_used = 0;
   c->prof_steps = 0;
+  return CLBM_OK;
+}
+
+extern "C" int clbm_profile_read_fields(clbm_ctx *c, double *field_ms, int *nintervals) {
+  if (!c || !field_ms || !nintervals) return fail(CLBM_ERR_INVALID, "NULL argument");
+  CK(cudaStreamSynchronize(c->stream));
+  double total = 0.0;
+  for (int i = 0; i + 1 < c->fev_used; i += 2) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->fev[i], c->fev[i + 1]));
+    total += ms;
+  }
+  *field_ms = total;
+  *nintervals = c->fev_used / 2;
+  c->fev_used = 0;
   return CLBM_OK;
 }
 
@@ -1493,7 +1534,7 @@ extern "C" int clbm_ref_random_field(int dx, int dy, double sigma, unsigned long
   cudaError_t e = cudaMemcpyAsync((char *)c->d.state + offsetof(RunState, interval), &draw, sizeof(int),
                                   cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) {
-    FieldArgs fa{c->d.runs, c->nruns, c->d.state, c->d_spec, c->d_tw, c->d_ybuf, c->d_maps};
+    FieldArgs fa{c->d.runs, c->nruns, c->d.state, c->d_spec, c->d_tw, c->d_ybuf, c->d_maps, c->d_fa, c->d.err};
     e = launch_fields(fa, c->total_clones, c->field_max_w, c->field_max_m1, c->field_max_m2,
                       c->field_max_tiles2, c->stream);
   }

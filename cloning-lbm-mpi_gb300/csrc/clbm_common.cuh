@@ -32,6 +32,7 @@ enum : unsigned {
   ERR_BAD_DENSITY = 1u << 2,
   ERR_BAD_PARENT = 1u << 3,
   ERR_RESAMPLE = 1u << 4,
+  ERR_TIMEOUT = 1u << 5,
 };
 
 // Body-force terms of the FP32 collision for one value of beta:
@@ -137,6 +138,8 @@ struct RunDev {
   long long spec_base;         // offset of the sqrt-spectrum (M1*M2 floats)
   long long tw1_base, tw2_base;// offsets of the twiddle tables (complex floats)
   long long y_base;            // offset of the stage-1 buffer (W*M2 complex per clone)
+  long long fa_base;           // float offset of the stage-1 DFT operand image (tensor cores)
+  int f_mpad, f_kchunks;       // its rows (2W rounded up to 128) and 32-wide K chunks
 };
 
 // Bounce-back classification of node (x,y): bit k set means the outgoing

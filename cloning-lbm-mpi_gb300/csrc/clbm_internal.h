@@ -58,8 +58,10 @@ struct FieldArgs {
   const RunState *state;   // interval counter (random-stream counter)
   const float *spec;       // sqrt spectra, [M1][M2] per field run
   const float2 *twiddles;  // exp(-2 pi i k / M1), exp(-2 pi i k / M2) per field run
-  float2 *ybuf;            // stage-1 results, [W][M2] per clone
+  float2 *ybuf;            // stage-1 results: [2][W][M2] floats per clone (real, imaginary planes)
   float *maps;             // fields, W*H per clone, node order y*W + x
+  const float *dft;        // stage-1 DFT operand images (tensor-core layout), per field run
+  unsigned *err;           // device error word
 };
 
 struct StepArgs {
@@ -131,6 +133,12 @@ cudaError_t launch_reconstruct(const double *hist_drag, const int *hist_labels, 
                                int *anc, double *out, cudaStream_t s);
 cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int max_m1, int max_m2,
                           int max_tiles2, cudaStream_t s);
+// rows of the tensor-core stage-1 operand (2W rounded up to the 128-row tile)
+// and its 32-wide K chunks (2 M1 rounded up); the image holds
+// mpad * 32 * kchunks floats
+inline int field_dft_mpad(int W) { return (2 * W + 127) / 128 * 128; }
+inline int field_dft_kchunks(int M1) { return (2 * M1 + 31) / 32; }
+void build_field_dft_image(int W, int M1, int mpad, int kchunks, float *out);
 cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W, int H,
                             cudaStream_t s);
 int temporal_max_clusters(int cs, int variant, int W, int H, bool field);

@@ -48,6 +48,8 @@ extern "C" {
 #define CLBM_DEV_BAD_DENSITY 0x4u     /* rho <= 0 or NaN at some node */
 #define CLBM_DEV_BAD_PARENT 0x8u      /* resampling produced an invalid parent */
 #define CLBM_DEV_RESAMPLE 0x10u       /* copy numbers could not be corrected */
+#define CLBM_DEV_TIMEOUT 0x20u        /* a bounded wait of the random-field
+                                         tensor-core kernel gave up */
 
 /* arithmetic of the populations */
 #define CLBM_FP64 0 /* FP64, reference operation order, no fused multiply-add */
@@ -266,6 +268,10 @@ int clbm_run_sampler(clbm_ctx *ctx, int steps, int intervals, double *rvalues);
  * and the number of LB steps they cover (and resets them). */
 int clbm_profile(clbm_ctx *ctx, int enable);
 int clbm_profile_read(clbm_ctx *ctx, double *step_ms, int *nsteps);
+/* the same for the random-field kernels (forcing variant): summed
+ * milliseconds of the field draws of the profiled intervals and their number
+ * (and resets them) */
+int clbm_profile_read_fields(clbm_ctx *ctx, double *field_ms, int *nintervals);
 
 /* Autotuner of the FP32 interval: times each candidate on this context's
  * workload at an interval boundary without touching the sampler state, and

@@ -57,6 +57,64 @@ def test_field_covariance_and_determinism(gpu, clbm_lib, orc):
     assert abs(f.mean()) < 0.03
 
 
+def philox4x32_10(c0, c1, c2, c3, seed):
+    """Philox4x32-10 (Salmon et al., SC'11), vectorised over counter arrays."""
+    M = np.uint64(0xFFFFFFFF)
+    c = [np.asarray(v, dtype=np.uint64) & M for v in (c0, c1, c2, c3)]
+    k0, k1 = np.uint64(seed & 0xFFFFFFFF), np.uint64(seed >> 32)
+    for _ in range(10):
+        p0 = np.uint64(0xD2511F53) * c[0]
+        p1 = np.uint64(0xCD9E8D57) * c[2]
+        c = [((p1 >> np.uint64(32)) ^ c[1] ^ k0) & M, p1 & M, ((p0 >> np.uint64(32)) ^ c[3] ^ k1) & M, p0 & M]
+        k0 = (k0 + np.uint64(0x9E3779B9)) & M
+        k1 = (k1 + np.uint64(0xBB67AE85)) & M
+    return c
+
+
+def field_fp64(W, H, sigma, seed, clone, interval, run=0):
+    """The device's field of (clone, interval) recomputed in FP64: the same
+    Philox counters and Box-Muller normals, then map = Re(F1 (s Z) F2) over
+    the embedding (the two contractions of the device stages)."""
+    lam, M1, M2 = embedding_spectrum(W, H, sigma)
+    s = np.sqrt(np.maximum(lam, 0.0))
+    s = s.astype(np.float32).astype(np.float64)  # the device keeps sqrt(lambda) in FP32
+    a, b = np.meshgrid(np.arange(M1), np.arange(M2), indexing="ij")
+    c = philox4x32_10(a * M2 + b, np.full(a.shape, clone), np.full(a.shape, interval),
+                      np.full(a.shape, (run << 4) | 4), seed)
+    u1 = (c[0].astype(np.float64) + 1.0) * 2.0 ** -32
+    u2 = c[1].astype(np.float64) * 2.0 ** -32
+    rad = s * np.sqrt(-2.0 * np.log(u1))
+    Z = np.where(s != 0, rad * np.exp(2j * np.pi * u2), 0)
+    F1 = np.exp(-2j * np.pi * np.outer(np.arange(W), np.arange(M1)) / M1)
+    F2 = np.exp(-2j * np.pi * np.outer(np.arange(M2), np.arange(H)) / M2)
+    return np.real(F1 @ Z @ F2)  # [x][y]
+
+
+@pytest.mark.parametrize("W,H,sig", [(40, 24, 3.0), (200, 80, 12.0), (300, 20, 32.0)])
+def test_field_transform_against_fp64(gpu, clbm_lib, orc, W, H, sig):
+    """The tensor-core stage 1 (TF32 operands, FP32 accumulation) and stage 2
+    against the same fields in FP64: every value within 4e-3 of the fields'
+    RMS (TF32 keeps 11 significant bits of the operands).  The lattices cover
+    one 128-row tile, four tiles with two column tiles (M2 = 159), and two
+    passes of row tiles (2W = 600)."""
+    g = orc.channel_geom(W, H, 4, W // 4, H // 2)
+    nc, seed = 3, 17
+    d = run_desc(clbm_lib, g, nc, tau=0.6, beta=1e-6, field_mode=1, field_steps=1, field_eps=0.1,
+                 field_sigma=sig, seed=seed, force_scale=1.0, dt=1.0)
+    with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=2) as s:
+        s.init_equilibrium(0, 0.02, 1e-3, 1)
+        for t in range(2):
+            s.run_interval(2)
+            for j in range(nc):
+                got = s.field_map(0, j)[0].reshape(W, H)
+                ref = field_fp64(W, H, sig, seed, j, t)
+                rms = np.sqrt(np.mean(ref ** 2))
+                assert rms > 0.1
+                assert np.abs(got - ref).max() < 4e-3 * rms, (t, j, np.abs(got - ref).max() / rms)
+            s.clone_step()
+        assert s.error_word() == 0
+
+
 def test_spatial_force_stepping_matches_oracle(gpu, clbm_lib, orc):
     W, H, side, nc, T1, T2 = 48, 20, 5, 3, 6, 5
     g = orc.channel_geom(W, H, side, 12, 10)
