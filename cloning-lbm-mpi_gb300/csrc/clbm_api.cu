@@ -89,6 +89,7 @@ struct clbm_ctx {
   float *d_spec = nullptr, *d_maps = nullptr;
   float2 *d_tw = nullptr, *d_ybuf = nullptr;
   float *d_fa = nullptr;  // stage-1 DFT operand images of the field runs
+  int *d_flist = nullptr; // kept embedding rows and columns of the field runs
   int field_max_w = 0, field_max_m1 = 0, field_max_m2 = 0, field_max_tiles2 = 0;
   std::vector<int> field_negative;  // spectrum entries below -1e-15 (clamped to 0)
   // lineage history (clbm_enable_history)
@@ -174,7 +175,7 @@ extern "C" int clbm_destroy(clbm_ctx *c) {
                   c->d.pert, c->d.partials, c->d.scratch_i, c->d.scratch_d, c->d.snaps,
                   c->d.rvalues, c->d.logr, c->d.err, c->d.terms, c->d_identity, c->d_zeros,
                   c->adj.s0, c->adj.ckpt, c->adj.seg, c->adj.sig[0], c->adj.sig[1],
-                  c->hist_drag, c->hist_labels, c->d_spec, c->d_maps, c->d_tw, c->d_ybuf, c->d_fa};
+                  c->hist_drag, c->hist_labels, c->d_spec, c->d_maps, c->d_tw, c->d_ybuf, c->d_fa, c->d_flist};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -230,8 +231,9 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
   c->desc.assign(runs, runs + nruns);
   c->snaps_loaded.assign(nruns, 0);
   c->runs_h.resize(nruns);
-  long long pop = 0, terms = 0, snaps = 0, spec = 0, tw = 0, ybuf = 0, maps = 0, fa = 0;
+  long long pop = 0, terms = 0, snaps = 0, spec = 0, tw = 0, ybuf = 0, maps = 0, fa = 0, flist = 0;
   std::vector<float> h_fa;
+  std::vector<int> h_flist;
   std::vector<float> h_spec;
   std::vector<float2> h_tw;
   c->field_negative.assign(nruns, 0);
@@ -318,6 +320,23 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
         return l;
       };
       const std::vector<double> l1 = spectrum(M1), l2 = spectrum(M2);
+      // The modes kept.  lambda[a][b] = l1[a] l2[b] / (M1 M2), so a row a whose
+      // |l1[a]| is below 1e-16 of the largest has every amplitude sqrt(lambda)
+      // below 1e-8 of the largest, and likewise a column b.  Left out, all such
+      // modes together (at most M1 M2 of them, independent normals) change the
+      // field by under 3e-6 of its RMS -- far below the TF32 rounding of the
+      // transform.  A smooth field (sigma of the order of the lattice) keeps a
+      // few percent of the rows and columns; a rough one keeps them all.
+      auto kept = [](const std::vector<double> &l) {
+        double mx = 0.0;
+        for (double v : l) mx = std::max(mx, std::fabs(v));
+        std::vector<int> idx;
+        for (int i = 0; i < (int)l.size(); i++)
+          if (std::fabs(l[i]) > 1e-16 * mx) idx.push_back(i);
+        return idx;
+      };
+      const std::vector<int> alist = kept(l1), blist = kept(l2);
+      const int na = (int)alist.size(), nb = (int)blist.size();
       R.field_mode = 1;
       R.field_steps = d.field_steps;
       R.M1 = M1;
@@ -328,28 +347,37 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
       R.tw1_base = tw;
       R.tw2_base = tw + M1;
       R.y_base = ybuf;
+      R.fna = na;
+      R.fnb = nb;
+      R.flist_base = flist;
+      h_flist.insert(h_flist.end(), alist.begin(), alist.end());
+      h_flist.insert(h_flist.end(), blist.begin(), blist.end());
+      flist += na + nb;
       R.f_mpad = field_dft_mpad(d.width);
-      R.f_kchunks = field_dft_kchunks(M1);
+      R.f_kchunks = field_dft_kchunks(na);
       R.fa_base = fa;
       h_fa.resize(fa + (size_t)R.f_mpad * 32 * R.f_kchunks);
-      build_field_dft_image(d.width, M1, R.f_mpad, R.f_kchunks, h_fa.data() + fa);
+      build_field_dft_image(d.width, M1, alist.data(), na, R.f_mpad, R.f_kchunks, h_fa.data() + fa);
       fa += (long long)R.f_mpad * 32 * R.f_kchunks;
       R.map_base = maps;
-      h_spec.resize(spec + (size_t)M1 * M2);
       for (int a = 0; a < M1; a++)
-        for (int b = 0; b < M2; b++) {
-          const double lam = l1[a] * l2[b] / ((double)M1 * M2);
-          if (lam < -1e-15) c->field_negative[r]++;
-          h_spec[spec + (size_t)a * M2 + b] = lam > 0 ? (float)std::sqrt(lam) : 0.f;
+        for (int b = 0; b < M2; b++)
+          if (l1[a] * l2[b] / ((double)M1 * M2) < -1e-15) c->field_negative[r]++;
+      // sqrt(lambda) of the kept modes, [a index][b index]
+      h_spec.resize(spec + (size_t)na * nb);
+      for (int j = 0; j < na; j++)
+        for (int jb = 0; jb < nb; jb++) {
+          const double lam = l1[alist[j]] * l2[blist[jb]] / ((double)M1 * M2);
+          h_spec[spec + (size_t)j * nb + jb] = lam > 0 ? (float)std::sqrt(lam) : 0.f;
         }
       h_tw.resize(tw + M1 + M2);
       for (int k = 0; k < M1; k++)
         h_tw[tw + k] = make_float2((float)std::cos(2.0 * M_PI * k / M1), (float)-std::sin(2.0 * M_PI * k / M1));
       for (int k = 0; k < M2; k++)
         h_tw[tw + M1 + k] = make_float2((float)std::cos(2.0 * M_PI * k / M2), (float)-std::sin(2.0 * M_PI * k / M2));
-      spec += (long long)M1 * M2;
+      spec += (long long)na * nb;
       tw += M1 + M2;
-      ybuf += (long long)d.nclones * d.width * M2;
+      ybuf += (long long)d.nclones * d.width * nb;
       maps += (long long)d.nclones * R.nodes;
       c->any_field = true;
       c->field_max_w = std::max(c->field_max_w, d.width);
@@ -418,6 +446,8 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
     if ((e = dalloc(c->d_tw, (size_t)tw)) != cudaSuccess) return bail(e);
     if ((e = dalloc(c->d_ybuf, (size_t)ybuf)) != cudaSuccess) return bail(e);
     if ((e = dalloc(c->d_fa, (size_t)fa)) != cudaSuccess) return bail(e);
+    if ((e = dalloc(c->d_flist, (size_t)flist)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemcpy(c->d_flist, h_flist.data(), sizeof(int) * flist, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e);
     if ((e = cudaMemcpy(c->d_fa, h_fa.data(), sizeof(float) * fa, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e);
     if ((e = dalloc(c->d_maps, (size_t)maps)) != cudaSuccess) return bail(e);
     if ((e = cudaMemcpy(c->d_spec, h_spec.data(), sizeof(float) * spec, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e);
@@ -717,7 +747,7 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
       }
       if ((e = cudaEventRecord(c->fev[c->fev_used], s)) != cudaSuccess) return e;
     }
-    FieldArgs fa{c->d.runs, c->nruns, c->d.state, c->d_spec, c->d_tw, c->d_ybuf, c->d_maps, c->d_fa, c->d.err};
+    FieldArgs fa{c->d.runs, c->nruns, c->d.state, c->d_spec, c->d_tw, c->d_ybuf, c->d_maps, c->d_fa, c->d.err, c->d_flist};
     e = launch_fields(fa, c->total_clones, c->field_max_w, c->field_max_m1, c->field_max_m2,
                       c->field_max_tiles2, s);
     if (e != cudaSuccess) return e;
@@ -1534,7 +1564,7 @@ extern "C" int clbm_ref_random_field(int dx, int dy, double sigma, unsigned long
   cudaError_t e = cudaMemcpyAsync((char *)c->d.state + offsetof(RunState, interval), &draw, sizeof(int),
                                   cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) {
-    FieldArgs fa{c->d.runs, c->nruns, c->d.state, c->d_spec, c->d_tw, c->d_ybuf, c->d_maps, c->d_fa, c->d.err};
+    FieldArgs fa{c->d.runs, c->nruns, c->d.state, c->d_spec, c->d_tw, c->d_ybuf, c->d_maps, c->d_fa, c->d.err, c->d_flist};
     e = launch_fields(fa, c->total_clones, c->field_max_w, c->field_max_m1, c->field_max_m2,
                       c->field_max_tiles2, c->stream);
   }

@@ -140,6 +140,8 @@ struct RunDev {
   long long y_base;            // offset of the stage-1 buffer (W*M2 complex per clone)
   long long fa_base;           // float offset of the stage-1 DFT operand image (tensor cores)
   int f_mpad, f_kchunks;       // its rows (2W rounded up to 128) and 32-wide K chunks
+  int fna, fnb;                // modes kept: rows a of the embedding, columns b
+  long long flist_base;        // offset of their index lists (a list, then b list)
 };
 
 // Bounce-back classification of node (x,y): bit k set means the outgoing

@@ -36,6 +36,15 @@
 // hand-off).  The four 128-row tiles of a pass accumulate in 4 x 128 columns
 // of tensor memory.  TF32 keeps 11 significant bits of the operands; the
 // field's covariance tests bound the effect.
+//
+// Only the embedding's significant modes enter: lambda is separable, and the
+// rows a and columns b whose 1-D eigenvalue lies below 1e-16 of the largest
+// are left out (their amplitudes are below 1e-8 of the largest; together they
+// move the field by under 3e-6 of its RMS).  The sums over a and b above run
+// over the kept lists; every kept mode draws its normal from the same Philox
+// counter (a M2 + b, clone, interval, run) as in the full transform.  For the
+// reference's sigma = 32 on a 256 x 64 lattice this keeps 43 of 511 rows and
+// 11 of 127 columns.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -77,9 +86,11 @@ __device__ __forceinline__ unsigned long long smem_desc(unsigned addr) {
          ((unsigned long long)(1024u >> 4) << 32) | (1ull << 46);
 }
 
-// instruction descriptor: D FP32, A and B TF32, both K-major, N = 128, M = 128
-constexpr unsigned IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(NT >> 3) << 17) |
-                           ((unsigned)(MT >> 4) << 24);
+// instruction descriptor: D FP32, A and B TF32, both K-major, M = 128, N = n
+// (a multiple of 16 up to 256)
+__device__ __forceinline__ unsigned idesc(int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(n >> 3) << 17) | ((unsigned)(MT >> 4) << 24);
+}
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -109,10 +120,11 @@ __device__ __forceinline__ void bulk_load(unsigned dst, const void *src, unsigne
                "l"(src), "r"(bytes), "r"(bar)
                : "memory");
 }
-__device__ __forceinline__ void mma_tf32(unsigned d, unsigned long long a, unsigned long long b, unsigned acc) {
+__device__ __forceinline__ void mma_tf32(unsigned d, unsigned long long a, unsigned long long b, unsigned id,
+                                         unsigned acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d),
-      "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+      "l"(a), "l"(b), "r"(id), "r"(acc)
       : "memory");
 }
 __device__ __forceinline__ void mma_commit(unsigned bar) {
@@ -139,7 +151,8 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, float v[16]) {
 }  // namespace tc
 
 // Stage 1 on the tensor cores, one CTA per clone: every (pass of four 128-row
-// tiles, 128-column tile) unit runs the whole K loop in 32-wide chunks.
+// tiles, column tile of up to 128 kept columns) unit runs the whole K loop in
+// 32-wide chunks (16 kept rows a each).
 __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a) {
   using namespace tc;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -147,10 +160,11 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
   const int r = field_run(a.runs, a.nruns, g);
   const RunDev &R = a.runs[r];
   if (R.field_mode == 0) return;
-  const int W = R.W, M1 = R.M1, M2 = R.M2;
+  const int W = R.W, M2 = R.M2, na = R.fna, nb = R.fnb;
   const int clone = g - R.clone_base;
   const int interval = a.state[r].interval;
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+  const int *alist = a.flist + R.flist_base, *blist = alist + na;
   float *A_s[2] = {(float *)smem, (float *)(smem + A_BYTES)};
   float *B_s[2] = {(float *)(smem + 2 * A_BYTES), (float *)(smem + 2 * A_BYTES + B_BYTES)};
   unsigned long long *bars = (unsigned long long *)(smem + 2 * A_BYTES + 2 * B_BYTES);
@@ -177,14 +191,16 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
   const unsigned tmem = tmem_base_s;
   const float *spec = a.spec + R.spec_base;
   const float *dft = a.dft + R.fa_base;
-  float *Yr = (float *)(a.ybuf + R.y_base) + (long long)clone * 2 * W * M2, *Yi = Yr + (long long)W * M2;
+  float *Yr = (float *)(a.ybuf + R.y_base) + (long long)clone * 2 * W * nb, *Yi = Yr + (long long)W * nb;
   const int ntiles_m = R.f_mpad / MT, passes = (ntiles_m + TILES - 1) / TILES;
-  const int ntiles_n = (M2 + NT - 1) / NT, nchunks = R.f_kchunks;
+  const int ntiles_n = (nb + NT - 1) / NT, nchunks = R.f_kchunks;
   int gc = 0;          // chunks issued by this CTA so far (buffer and mbarrier phase)
   bool ok = true;
   for (int unit = 0; unit < passes * ntiles_n; unit++) {
     const int pass = unit / ntiles_n, nt = unit % ntiles_n;
     const int tiles = min(TILES, ntiles_m - pass * TILES);
+    const int ncols = min(NT, nb - nt * NT), nmma = (ncols + 15) & ~15;  // MMA N: multiple of 16
+    const unsigned id = idesc(nmma);
     const float *dft_pass = dft + (long long)pass * TILES * nchunks * TILE_FLOATS;
     for (int c = 0; c < nchunks; c++, gc++) {
       const int buf = gc & 1, use = gc >> 1;
@@ -195,22 +211,25 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
         mbar_expect_tx(full_a[buf], bytes);
         bulk_load(smem_u32(A_s[buf]), dft_pass + (long long)c * tiles * TILE_FLOATS, bytes, full_a[buf]);
       }
-      // B chunk: rows n (b), K = 2a + q for a in [16c, 16c + 16), one
-      // complex draw per (a, b) written as the pair (k, k + 1).  The thread's
-      // sqrt(lambda) loads are issued first; the draws do not depend on them
-      // (a zero spectrum entry or a padding slot scales the draw to zero).
+      // B chunk: rows n (kept column), K = 2 j + q for kept rows j in
+      // [16c, 16c + 16), one complex draw per (a, b) = (alist[j], blist[n])
+      // written as the pair (k, k + 1).  The thread's sqrt(lambda) loads are
+      // issued first; the draws do not depend on them (a zero amplitude or a
+      // padding slot scales the draw to zero).
       float *B = B_s[buf];
       constexpr int PER = 16 * NT / THREADS;
       float sv[PER];
 #pragma unroll
       for (int j = 0; j < PER; j++) {
-        const int d = tid + j * THREADS, av = c * 16 + d / NT, b = nt * NT + d % NT;
-        sv[j] = (av < M1 && b < M2) ? __ldg(spec + (long long)av * M2 + b) : 0.0f;
+        const int d = tid + j * THREADS, jr = c * 16 + d / nmma, n = d % nmma, jc = nt * NT + n;
+        sv[j] = (d < 16 * nmma && jr < na && n < ncols) ? __ldg(spec + (long long)jr * nb + jc) : 0.0f;
       }
 #pragma unroll
       for (int j = 0; j < PER; j++) {
-        const int d = tid + j * THREADS, al = d / NT, n = d % NT;
-        const int av = c * 16 + al, b = nt * NT + n;
+        const int d = tid + j * THREADS;
+        if (d >= 16 * nmma) break;
+        const int al = d / nmma, n = d % nmma, jr = c * 16 + al, jc = nt * NT + n;
+        const int av = jr < na ? alist[jr] : 0, b = n < ncols ? blist[jc] : 0;
         uint32_t ctr[4] = {(uint32_t)(av * M2 + b), (uint32_t)clone, (uint32_t)interval,
                            (R.run_id << 4) | DOM_FIELD};
         philox4x32_10(ctr, (uint32_t)R.seed, (uint32_t)(R.seed >> 32));
@@ -234,7 +253,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
           for (int t = 0; t < tiles; t++)
 #pragma unroll
             for (int ks = 0; ks < KC / 8; ks++)
-              mma_tf32(tmem + t * NT, smem_desc(a0 + t * TILE_FLOATS * 4 + ks * 256), smem_desc(b0 + ks * 256),
+              mma_tf32(tmem + t * NT, smem_desc(a0 + t * TILE_FLOATS * 4 + ks * 256), smem_desc(b0 + ks * 256), id,
                        (c > 0 || ks > 0) ? 1u : 0u);
           mma_commit(mma_done[buf]);
         }
@@ -254,7 +273,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
     static_assert(THREADS == 512, "16 warps: 4 lane quarters x 4 column quarters");
     for (int t = 0; t < tiles; t++) {
       const int m = (pass * TILES + t) * MT + 32 * q + lane;
-      float *dst = m < W ? Yr + (long long)m * M2 : (m < 2 * W ? Yi + (long long)(m - W) * M2 : nullptr);
+      float *dst = m < W ? Yr + (long long)m * nb : (m < 2 * W ? Yi + (long long)(m - W) * nb : nullptr);
 #pragma unroll
       for (int j = 0; j < 2; j++) {
         const int n0 = 32 * h + 16 * j;
@@ -262,10 +281,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
         tmem_ld16(tmem + ((unsigned)(32 * q) << 16) + t * NT + n0, v);
         if (dst) {
 #pragma unroll
-          for (int i = 0; i < 16; i++) {
-            const int b = nt * NT + n0 + i;
-            if (b < M2) dst[b] = v[i];
-          }
+          for (int i = 0; i < 16; i++)
+            if (n0 + i < ncols) dst[nt * NT + n0 + i] = v[i];
         }
       }
     }
@@ -286,13 +303,15 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
 constexpr int F2_TX = 16, F2_TY = 16, F2_KB = 64;
 constexpr int F2_LD = F2_TX + 1;  // staging row length: the 32 threads of a store spread over 16 banks
 
+// Stage 2: map[x][y] = sum over the kept columns j of Re Y[x][j] w2^(b_j y)
+// = Yr cos + Yi sin (w2^(b y) = cos - i sin), 16 x 16 outputs per CTA.
 __global__ void __launch_bounds__(F2_TX *F2_TY) k_field_stage2(FieldArgs a) {
   extern __shared__ float2 sh[];
   const int g = blockIdx.y;
   const int r = field_run(a.runs, a.nruns, g);
   const RunDev &R = a.runs[r];
   if (R.field_mode == 0) return;
-  const int W = R.W, H = R.H, M2 = R.M2;
+  const int W = R.W, H = R.H, M2 = R.M2, nb = R.fnb;
   const int tilesx = (W + F2_TX - 1) / F2_TX;
   const int tile = blockIdx.x;
   if (tile >= tilesx * ((H + F2_TY - 1) / F2_TY)) return;
@@ -300,29 +319,49 @@ __global__ void __launch_bounds__(F2_TX *F2_TY) k_field_stage2(FieldArgs a) {
   const int clone = g - R.clone_base;
   float2 *tw = sh;             // M2 twiddles
   float2 *Ys = sh + M2;        // [F2_KB][F2_LD]: k-major, so the 16 x of a warp read 32 consecutive words
+  int *bs = (int *)(Ys + F2_KB * F2_LD);  // the chunk's kept columns b
   const float2 *tw_g = a.twiddles + R.tw2_base;
   for (int i = threadIdx.x; i < M2; i += F2_TX * F2_TY) tw[i] = tw_g[i];
-  const float *Y = (const float *)(a.ybuf + R.y_base) + (long long)clone * 2 * W * M2;  // Re rows, then Im rows
+  const int *blist = a.flist + R.flist_base + R.fna;
+  const float *Y = (const float *)(a.ybuf + R.y_base) + (long long)clone * 2 * W * nb;  // Re rows, then Im rows
   const int tx = threadIdx.x % F2_TX, ty = threadIdx.x / F2_TX;
   const int x = x0 + tx, y = y0 + ty;
   float acc = 0.f;
-  for (int bb = 0; bb < M2; bb += F2_KB) {
+  for (int jb = 0; jb < nb; jb += F2_KB) {
     __syncthreads();
     for (int i = threadIdx.x; i < F2_TX * F2_KB; i += F2_TX * F2_TY) {
-      const int xi = x0 + i / F2_KB, bi = bb + i % F2_KB;  // coalesced along b in Y
+      const int xi = x0 + i / F2_KB, j = jb + i % F2_KB;  // coalesced along j in Y
       const int si = (i % F2_KB) * F2_LD + i / F2_KB;
-      Ys[si] = (xi < W && bi < M2) ? make_float2(Y[(long long)xi * M2 + bi], Y[(long long)(W + xi) * M2 + bi])
-                                   : make_float2(0.f, 0.f);
+      Ys[si] = (xi < W && j < nb) ? make_float2(Y[(long long)xi * nb + j], Y[(long long)(W + xi) * nb + j])
+                                  : make_float2(0.f, 0.f);
     }
+    for (int i = threadIdx.x; i < F2_KB; i += F2_TX * F2_TY) bs[i] = jb + i < nb ? blist[jb + i] : 0;
     __syncthreads();
     if (x < W && y < H) {
-      const int kmax = min(F2_KB, M2 - bb);
-      int idx = (int)(((long long)bb * y) % M2);
+      // twiddle index (b y) mod M2, advanced by y along a run of consecutive
+      // kept columns (the kept columns form at most two runs)
+      const int kmax = min(F2_KB, nb - jb);
+      int prev = -2, idx = 0;
+      if (nb == M2) {  // every column kept: b = jb + k
+        idx = (int)(((unsigned)jb * (unsigned)y) % (unsigned)M2);
+        for (int k = 0; k < kmax; k++) {
+          const float2 t = tw[idx], v = Ys[k * F2_LD + tx];
+          acc = fmaf(v.x, t.x, fmaf(-v.y, t.y, acc));
+          idx += y;
+          if (idx >= M2) idx -= M2;
+        }
+      } else
       for (int k = 0; k < kmax; k++) {
+        const int b = bs[k];
+        if (b == prev + 1) {
+          idx += y;
+          if (idx >= M2) idx -= M2;
+        } else {
+          idx = (int)(((unsigned)b * (unsigned)y) % (unsigned)M2);
+        }
+        prev = b;
         const float2 t = tw[idx], v = Ys[k * F2_LD + tx];
         acc = fmaf(v.x, t.x, fmaf(-v.y, t.y, acc));
-        idx += y;
-        if (idx >= M2) idx -= M2;
       }
     }
   }
@@ -342,15 +381,16 @@ cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int m
   k_field_stage1_tc<<<total_clones, tc::THREADS, tc::SMEM, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const size_t sh2 = sizeof(float2) * ((size_t)max_m2 + F2_LD * F2_KB);
+  const size_t sh2 = sizeof(float2) * ((size_t)max_m2 + F2_LD * F2_KB) + sizeof(int) * F2_KB;
   dim3 g2(max_tiles2, total_clones);
   k_field_stage2<<<g2, F2_TX * F2_TY, sh2, s>>>(a);
   return cudaGetLastError();
 }
 
 // The stage-1 operand image of one run (see the head of this file), TF32
-// values in FP32 containers: out must hold mpad * 32 * kchunks floats.
-void build_field_dft_image(int W, int M1, int mpad, int kchunks, float *out) {
+// values in FP32 containers, columns k = 2 j + q for the kept rows
+// a = alist[j]: out must hold mpad * 32 * kchunks floats.
+void build_field_dft_image(int W, int M1, const int *alist, int na, int mpad, int kchunks, float *out) {
   using namespace tc;
   const int ntm = mpad / MT;
   for (int m = 0; m < mpad; m++) {
@@ -360,10 +400,10 @@ void build_field_dft_image(int W, int M1, int mpad, int kchunks, float *out) {
     const int tiles = std::min(TILES, ntm - pass * TILES);
     float *base = out + (long long)pass * TILES * kchunks * TILE_FLOATS;
     for (int k = 0; k < kchunks * KC; k++) {
-      const int av = k / 2, qi = k % 2;
+      const int j = k / 2, qi = k % 2;
       double v = 0.0;
-      if (part >= 0 && av < M1) {
-        const double th = 2.0 * M_PI * (double)(((long long)av * x) % M1) / M1;
+      if (part >= 0 && j < na) {
+        const double th = 2.0 * M_PI * (double)(((long long)alist[j] * x) % M1) / M1;
         const double c = std::cos(th), sn = std::sin(th);
         v = part == 0 ? (qi == 0 ? c : sn) : (qi == 0 ? -sn : c);
       }

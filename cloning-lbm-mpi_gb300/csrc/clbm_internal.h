@@ -62,6 +62,7 @@ struct FieldArgs {
   float *maps;             // fields, W*H per clone, node order y*W + x
   const float *dft;        // stage-1 DFT operand images (tensor-core layout), per field run
   unsigned *err;           // device error word
+  const int *flist;        // kept embedding rows a and columns b, per field run
 };
 
 struct StepArgs {
@@ -134,11 +135,11 @@ cudaError_t launch_reconstruct(const double *hist_drag, const int *hist_labels, 
 cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int max_m1, int max_m2,
                           int max_tiles2, cudaStream_t s);
 // rows of the tensor-core stage-1 operand (2W rounded up to the 128-row tile)
-// and its 32-wide K chunks (2 M1 rounded up); the image holds
+// and its 32-wide K chunks (twice the kept rows a, rounded up); the image holds
 // mpad * 32 * kchunks floats
 inline int field_dft_mpad(int W) { return (2 * W + 127) / 128 * 128; }
-inline int field_dft_kchunks(int M1) { return (2 * M1 + 31) / 32; }
-void build_field_dft_image(int W, int M1, int mpad, int kchunks, float *out);
+inline int field_dft_kchunks(int na) { return (2 * na + 31) / 32; }
+void build_field_dft_image(int W, int M1, const int *alist, int na, int mpad, int kchunks, float *out);
 cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W, int H,
                             cudaStream_t s);
 int temporal_max_clusters(int cs, int variant, int W, int H, bool field);

@@ -418,11 +418,21 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
   bool bad = false;
   cluster.sync();
   // every step but the last
+  // (steps past the field's run through the uniform-force path: with eps = 0
+  // the field path computes the same beta and constants bit for bit)
   for (int t = 0; t + 1 < a.steps; t++) {
-    if ((t & 1) == 0)
-      band_step<NW, true, FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
-    else
-      band_step<NW, false, FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
+    const bool field = FIELD && t + 1 < R.field_steps;
+    if ((t & 1) == 0) {
+      if (field)
+        band_step<NW, true, FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
+      else
+        band_step<NW, true, false>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
+    } else {
+      if (field)
+        band_step<NW, false, FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
+      else
+        band_step<NW, false, false>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
+    }
     cluster.sync();
   }
   // the last step stores S_T (one step in T: every node through update_general)
