@@ -364,6 +364,10 @@ def adjoint_study(args, wl, directions: int = 32, every: int = 20, eps: float = 
             grads[name] = np.concatenate([s.drag_grad(0, j) for j in range(r.nclones)])
             out[name] = {"fwd_s": t1 - t0, "bwd_s": t2 - t1, "J_mean": float(np.mean(J))}
     errs = {"fp32": [], "fp64": []}
+    nerrs = {"fp32": [], "fp64": []}  # |ad - fd| / (|g| |d|) per clone and direction
+    cos_fd = []                       # |fd| / (|g| |d|): how far the direction is from orthogonal to g
+    g64 = grads["fp64"].reshape(r.nclones, n)
+    gnorm = np.linalg.norm(g64, axis=1)
     with clbm.Sampler(descs, clbm.FP64, max_steps=T) as f:
         for _ in range(directions):
             d = rng.normal(0.0, 1.0, base.size)
@@ -372,12 +376,24 @@ def adjoint_study(args, wl, directions: int = 32, every: int = 20, eps: float = 
             f.load_run(0, S0 - eps * d)
             jm = f.drag_fwd(T, every)
             fd = (jp - jm) / (2 * eps)
+            dn = np.linalg.norm(d.reshape(r.nclones, n), axis=1)
+            cos_fd.extend((np.abs(fd) / (gnorm * dn)).tolist())
             for k in errs:
                 ad = (grads[k] * d).reshape(r.nclones, n).sum(axis=1)
                 errs[k].extend((np.abs(ad - fd) / np.abs(fd)).tolist())
+                nerrs[k].extend((np.abs(ad - fd) / (gnorm * dn)).tolist())
+    cos_fd = np.array(cos_fd)
     for k in errs:
-        e = np.array(errs[k])
-        out[k].update({"rel_err_max": float(e.max()), "rel_err_median": float(np.median(e))})
+        e, ne = np.array(errs[k]), np.array(nerrs[k])
+        w = int(np.argmax(e))
+        g = grads[k].reshape(r.nclones, n)
+        out[k].update({"rel_err_max": float(e.max()), "rel_err_median": float(np.median(e)),
+                       "rel_err_p99": float(np.quantile(e, 0.99)),
+                       "worst": {"clone": w % r.nclones, "direction": w // r.nclones,
+                                 "fd_over_gnorm_dnorm": float(cos_fd[w])},
+                       "norm_rel_err_max": float(ne.max()), "norm_rel_err_median": float(np.median(ne)),
+                       "grad_rel_l2_vs_fp64_max": float((np.linalg.norm(g - g64, axis=1) / gnorm).max())})
+    out["fd_over_gnorm_dnorm"] = {"min": float(cos_fd.min()), "median": float(np.median(cos_fd))}
     lups = r.nclones * r.nodes * T
     line = {"study": "adjoint", "workload": wl.name, "directions": directions, "fd_eps": eps,
             "checkpoint_every": every, "perturbation_sigma": r.noise, "comparisons": len(errs["fp32"]),

@@ -1,8 +1,15 @@
 """The hand-written adjoint of the interval-integrated drag against central
 finite differences of the FP64 forward (the forward is the sampler's own,
-bit-identical to the oracle).  Tolerances: FP64 adjoint within 1e-6 of the
-FD directional derivative (FD truncation and rounding are far below);
-FP32 adjoint within 2e-3 (FP32 forward recomputation and FP32 adjoint)."""
+bit-identical to the oracle).
+
+A directional derivative g.d along a random direction d can lie arbitrarily
+close to zero (g.d / (|g| |d|) is about N(0, 1/n) for n populations), where
+its relative error means nothing; the tolerances are therefore stated on the
+error relative to |g| |d| (FP64 adjoint 1e-10, FP32 1e-6, the FP32 forward
+recomputation and adjoint), on the relative error of the directions whose
+derivative is not near zero (|g.d| >= 0.1 |g| |d| / sqrt(n): FP64 1e-6, FP32
+5e-4), and, for FP32, on the whole gradient against the FP64 adjoint's
+(relative L2 distance 1e-5)."""
 import numpy as np
 import pytest
 
@@ -32,8 +39,7 @@ def test_forward_drag_matches_oracle(gpu, clbm_lib, orc):
 
 
 @pytest.mark.parametrize("drag_mode", [0, 1])
-@pytest.mark.parametrize("prec,tol", [(0, 1e-6), (1, 2e-3)])
-def test_adjoint_vs_central_differences(gpu, clbm_lib, orc, prec, tol, drag_mode):
+def test_adjoint_vs_central_differences(gpu, clbm_lib, orc, drag_mode):
     """drag_mode 0: the reference's stress integration; 1: momentum exchange."""
     g, phys, d = case(orc, clbm_lib)
     d.drag_mode = drag_mode
@@ -42,23 +48,31 @@ def test_adjoint_vs_central_differences(gpu, clbm_lib, orc, prec, tol, drag_mode
     rng = np.random.default_rng(5)
     base = np.concatenate([orc.init_equilibrium(g, 0.05, 1e-3, 5, 0, j) for j in range(nc)])
     S0 = base + rng.normal(0.0, 1e-4, base.size)
-    with clbm_lib.Sampler([d], prec, max_steps=T) as s:
-        s.load_run(0, S0)
-        s.drag_fwd(T, every)
-        s.drag_bwd()
-        grad = np.concatenate([s.drag_grad(0, j) for j in range(nc)])
-    assert np.isfinite(grad).all() and np.abs(grad).max() > 0
+    grad = {}
+    for prec in (clbm_lib.FP64, clbm_lib.FP32):
+        with clbm_lib.Sampler([d], prec, max_steps=T) as s:
+            s.load_run(0, S0)
+            s.drag_fwd(T, every)
+            s.drag_bwd()
+            grad[prec] = np.concatenate([s.drag_grad(0, j) for j in range(nc)]).reshape(nc, n)
+    g64, g32 = grad[clbm_lib.FP64], grad[clbm_lib.FP32]
+    gnorm = np.linalg.norm(g64, axis=1)
+    assert np.isfinite(g32).all() and (gnorm > 0).all()
+    assert (np.linalg.norm(g32 - g64, axis=1) / gnorm < 1e-5).all()
     with clbm_lib.Sampler([d], clbm_lib.FP64, max_steps=T) as f:
-        for _ in range(3):
+        for _ in range(4):
             dirn = rng.normal(0.0, 1.0, base.size)
             f.load_run(0, S0 + eps * dirn)
             jp = f.drag_fwd(T, every)
             f.load_run(0, S0 - eps * dirn)
             jm = f.drag_fwd(T, every)
             fd = (jp - jm) / (2 * eps)
-            ad = (grad * dirn).reshape(nc, n).sum(axis=1)
-            err = np.abs(ad - fd) / np.abs(fd)
-            assert (err < tol).all(), (err, ad, fd)
+            dn = np.linalg.norm(dirn.reshape(nc, n), axis=1)
+            well = np.abs(fd) >= 0.1 * gnorm * dn / np.sqrt(n)
+            for gr, tol_norm, tol_rel in ((g64, 1e-10, 1e-6), (g32, 1e-6, 5e-4)):
+                ad = (gr * dirn.reshape(nc, n)).sum(axis=1)
+                assert (np.abs(ad - fd) / (gnorm * dn) < tol_norm).all(), (ad, fd)
+                assert (np.abs(ad - fd)[well] / np.abs(fd)[well] < tol_rel).all(), (ad, fd)
 
 
 def test_adjoint_rejects_random_field_runs(gpu, clbm_lib, orc):
