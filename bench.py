@@ -354,7 +354,8 @@ def adjoint_study(args, wl, directions: int = 32, every: int = 20, eps: float = 
     for name, prec in (("fp32", clbm.FP32), ("fp64", clbm.FP64)):
         with clbm.Sampler(descs, prec, max_steps=T) as s:
             s.load_run(0, S0)
-            s.drag_fwd(T, every)  # warm-up
+            s.drag_fwd(T, every)  # warm-up of both passes (kernel loading)
+            s.drag_bwd()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             J = s.drag_fwd(T, every)
