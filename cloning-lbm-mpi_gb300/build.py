@@ -64,6 +64,28 @@ def build_library(verbose: bool = False) -> Path:
     return lib
 
 
+CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+
+
+def build_shim(verbose: bool = False) -> Path:
+    """libclbm_refshim.a: the reference's LBM and perturbation functions with
+    their own C++ signatures over libclbm (shim/clbm_refshim.cpp).  A program
+    links it as  libclbm_refshim.a -lclbm -lcudart  in place of the
+    reference's LBM objects."""
+    BUILD.mkdir(exist_ok=True)
+    src = PKG / "shim" / "clbm_refshim.cpp"
+    obj, lib = BUILD / "clbm_refshim.o", BUILD / "libclbm_refshim.a"
+    if _stale(lib, [src, REPO / "include" / "clbm.h"]):
+        _run([CXX, "-std=c++17", "-O2", "-fPIC", "-I", str(REPO / "include"), "-I", str(CUDA_HOME / "include"),
+              "-c", str(src), "-o", str(obj)])
+        if lib.exists():
+            lib.unlink()
+        _run(["ar", "rcs", str(lib), str(obj)])
+    if verbose:
+        print(f"built {lib}")
+    return lib
+
+
 DRIVER_VARIANTS = (("TLGK_LBM", "plain"), ("TLGK_LBM_POPS_PERTURB", "pops"),
                    ("TLGK_LBM_FORCING", "forcing"))
 
@@ -104,6 +126,7 @@ def main() -> None:
     build_library(verbose=True)
     if not a.lib_only:
         build_drivers(verbose=True)
+        build_shim(verbose=True)
 
 
 if __name__ == "__main__":
