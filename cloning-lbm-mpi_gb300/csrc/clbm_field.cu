@@ -372,14 +372,11 @@ cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int m
                           int max_tiles2, cudaStream_t s) {
   (void)max_w;
   (void)max_m1;
-  static bool configured = false;  // the attribute is per device function; set once per process
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_field_stage1_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  // (set on every launch: the attribute belongs to the current device)
+  cudaError_t e = cudaFuncSetAttribute(k_field_stage1_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM);
+  if (e != cudaSuccess) return e;
   k_field_stage1_tc<<<total_clones, tc::THREADS, tc::SMEM, s>>>(a);
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const size_t sh2 = sizeof(float2) * ((size_t)max_m2 + F2_LD * F2_KB) + sizeof(int) * F2_KB;
   dim3 g2(max_tiles2, total_clones);

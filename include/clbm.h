@@ -168,7 +168,9 @@ int clbm_ref_perturbed_state(double *fin, const double *snaps, double eps,
  * of 66 KB that every GPU loading the library holds until exit, so n (the
  * values of one state, 9*Dx*Dy) is limited to 1048576 and nsnap to 64; larger
  * sizes return CLBM_ERR_INVALID.  The first call on a device looks up the
- * array's device address, so make that first call before any stream capture.
+ * array's device address, so make that first call before any stream capture
+ * (the address is kept for the process: do not call it again after a
+ * cudaDeviceReset of that device).
  * Each call synchronises `stream` before it returns.  All calls share the
  * array: calls that overlap on the GPU (other streams, other host threads)
  * race and must be serialised by the caller. */
