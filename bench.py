@@ -529,6 +529,7 @@ def main():
         t0 = time.perf_counter()
         for i in range(len(wl.runs)):
             clbm.check(clbm.lib().clbm_load_run_aos_f64(s.h, i, host[i].data_ptr()), "load")
+        load_s = time.perf_counter() - t0
         h2d = sum(h.numel() * 8 for h in host)
         for _ in range(args.steps):
             # one interval and its cloning step (a CUDA graph unless --eager)
@@ -543,6 +544,7 @@ def main():
         wall = allmax(world, time.perf_counter() - t0)
         e2e = {"value": world * lups_interval * args.steps / wall, "unit": "clone-LUPS/s",
                "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
+               "initial_load": {"ms": 1e3 * load_s, "gb_per_s": h2d / load_s / 1e9},
                "note": "initial AoS FP64 populations from pinned host memory (amortised over the "
                        "steps) + per-interval drag series, labels, weights, copy numbers, R_t"}
 
