@@ -33,7 +33,19 @@ struct AdjArgs {
   const void *P;         // P_{t-1} (pulled into S_t), or S_0 when from_s0
   int with_drag;         // add kappa grad D(S_t)
   int from_s0;
+  int t;                 // the collision C(S_t) -> P_t: under the random field when t < field_steps
+  const float *maps;     // random body-force fields (nullable)
 };
+
+// body force of the collision C(S_t) at node n of a clone: beta (1 + eps map)
+// while the run's field acts (t < field_steps), else beta, as the forward
+template <typename T>
+__device__ __forceinline__ T adj_beta(const RunDev &R, const AdjArgs &a, int clone, int n) {
+  if (!(R.field_mode && a.maps && a.t < R.field_steps)) return (T)R.beta;
+  const float m = a.maps[R.map_base + (long long)clone * R.nodes + n];
+  if (sizeof(T) == 8) return (T)(R.beta * (1.0 + R.field_eps * (double)m));
+  return (T)field_beta_f32(R.f_beta, R.f_field_eps, m);
+}
 
 __device__ __forceinline__ int adj_locate(const RunDev *runs, int nruns, int &clone, int &n) {
   const int b = blockIdx.x;
@@ -89,9 +101,9 @@ __device__ __forceinline__ void drag_grad(const RunDev &R, int x, int y, const T
 //   Gy = omega rho (3 Py + 9 (ux Pxy + uy Pyy) - 3 uy P0) + 9 cf beta Pxy
 // (u2 = 1.5 |u|^2, cf the Guo prefactor, feq and F as in collide_ref64).
 template <typename T>
-__device__ __forceinline__ void collide_adjoint(const RunDev &R, const T S[9], const T pi[9],
+__device__ __forceinline__ void collide_adjoint(const RunDev &R, const T S[9], const T pi[9], T beta,
                                                 T out[9]) {
-  const T omega = (T)R.omega, om1 = T(1) - omega, beta = (T)R.beta;
+  const T omega = (T)R.omega, om1 = T(1) - omega;
   const T cf = (T)R.cforce;
   T sum = ((S[0] + (S[1] + S[3])) + (S[2] + S[4])) + ((S[5] + S[7]) + (S[6] + S[8]));
   const T rho = (sizeof(T) == 8 ? sum : T(1) + sum);
@@ -165,7 +177,7 @@ __global__ void __launch_bounds__(STEP_BLOCK) k_adj_step(AdjArgs a) {
     }
   }
   T o[9];
-  collide_adjoint<T>(R, S, pi, o);
+  collide_adjoint<T>(R, S, pi, adj_beta<T>(R, a, clone, n), o);
   if (a.with_drag && in_box) {
     T dg[9];
     drag_grad<T>(R, x, y, S, (T)(R.dt * R.force_scale), dg);
@@ -214,7 +226,7 @@ __global__ void __launch_bounds__(STEP_BLOCK) k_adj_init(AdjArgs a) {
 
 cudaError_t launch_adj_init(bool f64, const RunDev *runs, int nruns, const void *P, void *sigma,
                             int blocks, cudaStream_t s) {
-  AdjArgs a{runs, nruns, nullptr, sigma, P, 1, 0};
+  AdjArgs a{runs, nruns, nullptr, sigma, P, 1, 0, 0, nullptr};
   if (f64)
     k_adj_init<true><<<blocks, STEP_BLOCK, 0, s>>>(a);
   else
@@ -223,9 +235,9 @@ cudaError_t launch_adj_init(bool f64, const RunDev *runs, int nruns, const void 
 }
 
 cudaError_t launch_adj_step(bool f64, const RunDev *runs, int nruns, const void *sigma_in,
-                            void *sigma_out, const void *P, bool with_drag, bool from_s0,
-                            int blocks, cudaStream_t s) {
-  AdjArgs a{runs, nruns, sigma_in, sigma_out, P, with_drag ? 1 : 0, from_s0 ? 1 : 0};
+                            void *sigma_out, const void *P, bool with_drag, bool from_s0, int t,
+                            const float *maps, int blocks, cudaStream_t s) {
+  AdjArgs a{runs, nruns, sigma_in, sigma_out, P, with_drag ? 1 : 0, from_s0 ? 1 : 0, t, maps};
   if (f64)
     k_adj_step<true><<<blocks, STEP_BLOCK, 0, s>>>(a);
   else

@@ -1351,8 +1351,6 @@ extern "C" int clbm_drag_fwd(clbm_ctx *c, int steps, int every, double *J) {
   if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
   if (steps < 1 || steps > c->max_steps || every < 1) return fail(CLBM_ERR_INVALID, "bad steps / checkpoint period");
   if (c->pending) return fail(CLBM_ERR_INVALID, "a clone step is pending; run an interval first");
-  if (c->any_field)
-    return fail(CLBM_ERR_INVALID, "the adjoint covers the constant body force only (a run has a random field)");
   const bool f64 = c->precision == CLBM_FP64;
   const size_t pop = c->pop_elems * c->elem_size;
   const size_t nckpt = (size_t)(steps + every - 1) / every;
@@ -1370,14 +1368,16 @@ extern "C" int clbm_drag_fwd(clbm_ctx *c, int steps, int every, double *J) {
   auto loc = [&](int t) -> char * {
     return (t % every == 0) ? c->adj.ckpt + (size_t)(t / every) * pop : c->adj.sig[t % 2];
   };
+  // runs with a random body-force field step under the fields of the last
+  // interval (the ones clbm_get_field_map returns)
   ReseedArgs ra{c->d.runs, c->nruns, c->adj.s0, loc(0), c->d_identity, c->d_zeros, c->d.pert,
-                c->d.prefactors, c->d.snaps, c->d.state, c->d.err, nullptr};
+                c->d.prefactors, c->d.snaps, c->d.state, c->d.err, c->d_maps};
   CK(launch_reseed(f64, ra, c->total_blocks, s));
   for (int t = 0; t < steps; t++) {
     char *dst = (t + 1 < steps) ? loc(t + 1) : c->adj.sig[(t + 1) % 2];
     StepArgs a{c->d.runs, c->nruns, t, loc(t), dst, c->d.terms, c->d.term_slab, c->d.err,
                c->total_clones, c->max_nodes, {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]},
-               nullptr};
+               c->d_maps};
     CK(launch_step(f64, false, a, c->total_blocks, s, c->step_variant));
   }
   CK(launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, c->any_stress, c->any_momentum, s));
@@ -1404,10 +1404,10 @@ extern "C" int clbm_drag_bwd(clbm_ctx *c) {
   };
   for (int k = nseg - 1; k >= 0; k--) {
     const int lo = k * C, hi = std::min(lo + C, T) - 1;
-    for (int p = lo; p < hi; p++) {  // recompute P_lo .. P_hi from the checkpoint
-      StepArgs a{c->d.runs, c->nruns, 0, segP(lo, p), segP(lo, p + 1), c->d.terms, c->d.term_slab,
+    for (int p = lo; p < hi; p++) {  // recompute P_lo .. P_hi from the checkpoint (step p of the forward)
+      StepArgs a{c->d.runs, c->nruns, p, segP(lo, p), segP(lo, p + 1), c->d.terms, c->d.term_slab,
                  c->d.err, c->total_clones, c->max_nodes,
-                 {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}, nullptr};
+                 {c->total_tiles[0], c->total_tiles[1], c->total_tiles[2]}, c->d_maps};
       CK(launch_step(f64, false, a, c->total_blocks, s, c->step_variant));
     }
     for (int p = hi; p >= lo; p--) {
@@ -1415,13 +1415,13 @@ extern "C" int clbm_drag_bwd(clbm_ctx *c) {
         CK(launch_adj_init(f64, c->d.runs, c->nruns, segP(lo, p), c->adj.sig[cur], c->total_blocks, s));
       } else {
         CK(launch_adj_step(f64, c->d.runs, c->nruns, c->adj.sig[cur], c->adj.sig[1 - cur], segP(lo, p),
-                           true, false, c->total_blocks, s));
+                           true, false, p + 1, c->d_maps, c->total_blocks, s));
         cur = 1 - cur;
       }
     }
   }
   CK(launch_adj_step(f64, c->d.runs, c->nruns, c->adj.sig[cur], c->adj.sig[1 - cur], c->adj.s0, false,
-                     true, c->total_blocks, s));
+                     true, 0, c->d_maps, c->total_blocks, s));
   c->adj.result = 1 - cur;
   CK(cudaStreamSynchronize(s));
   return check_error_word(c);

@@ -123,8 +123,8 @@ cudaError_t launch_clone(const DevArrays &d, int nruns, cudaStream_t s);
 cudaError_t launch_adj_init(bool f64, const RunDev *runs, int nruns, const void *P, void *sigma,
                             int blocks, cudaStream_t s);
 cudaError_t launch_adj_step(bool f64, const RunDev *runs, int nruns, const void *sigma_in,
-                            void *sigma_out, const void *P, bool with_drag, bool from_s0,
-                            int blocks, cudaStream_t s);
+                            void *sigma_out, const void *P, bool with_drag, bool from_s0, int t,
+                            const float *maps, int blocks, cudaStream_t s);
 cudaError_t launch_hist_drag(const DevArrays &d, int total_clones, int steps, double *hist, int max_hist,
                              cudaStream_t s);
 cudaError_t launch_hist_labels(const DevArrays &d, int total_clones, int *hist, int max_hist,

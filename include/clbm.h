@@ -346,7 +346,8 @@ int clbm_reconstruct_lineages(clbm_ctx *ctx, int run, int *nintervals,
  * clone's gradient in the reference AoS layout (FP64, 9*Dx*Dy values; zero
  * inside the square).  dJ/dS_0 is the gradient with respect to an additive
  * perturbation of the populations.  Runs with a random body-force field
- * (field_mode) are not covered: clbm_drag_fwd returns CLBM_ERR_INVALID. */
+ * (field_mode) step, forward and backward, under the fields of the last
+ * interval (the ones clbm_get_field_map returns). */
 int clbm_drag_fwd(clbm_ctx *ctx, int steps, int every, double *J);
 int clbm_drag_bwd(clbm_ctx *ctx);
 int clbm_get_drag_grad_aos_f64(clbm_ctx *ctx, int run, int clone, double *aos);

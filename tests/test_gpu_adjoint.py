@@ -75,11 +75,43 @@ def test_adjoint_vs_central_differences(gpu, clbm_lib, orc, drag_mode):
                 assert (np.abs(ad - fd)[well] / np.abs(fd)[well] < tol_rel).all(), (ad, fd)
 
 
-def test_adjoint_rejects_random_field_runs(gpu, clbm_lib, orc):
+@pytest.mark.parametrize("prec", [0, 1])
+def test_adjoint_with_random_field(gpu, clbm_lib, orc, prec):
+    """A forcing-variant run: the forward and the adjoint step under the fields
+    of the last interval (drawn by one interval first), the field acting on
+    the first 12 of 30 steps; FD on the FP64 forward with the same fields."""
     g, phys, d = case(orc, clbm_lib)
-    d.field_mode, d.field_steps, d.field_eps, d.field_sigma = 1, 5, 0.2, 4.0
-    with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=10) as s:
+    d.field_mode, d.field_steps, d.field_eps, d.field_sigma = 1, 12, 0.3, 4.0
+    nc, T, every, eps = 3, 30, 7, 1e-6
+    n = 9 * g.nx * g.ny
+    rng = np.random.default_rng(9)
+    base = np.concatenate([orc.init_equilibrium(g, 0.05, 1e-3, 5, 0, j) for j in range(nc)])
+    S0 = base + rng.normal(0.0, 1e-4, base.size)
+
+    def sampler(p):
+        s = clbm_lib.Sampler([d], p, max_steps=T)
         s.init_equilibrium(0, 0.05, 1e-3, 1)
-        with pytest.raises(clbm_lib.ClbmError) as e:
-            s.drag_fwd(10, 5)
-        assert e.value.status == clbm_lib.ERR_INVALID
+        s.run_interval(T)  # draws the fields the forward and adjoint use
+        assert np.abs(s.field_map(0, 0)[0]).max() > 0.1
+        return s
+
+    with sampler(prec) as s:
+        s.load_run(0, S0)
+        s.drag_fwd(T, every)
+        s.drag_bwd()
+        grad = np.concatenate([s.drag_grad(0, j) for j in range(nc)]).reshape(nc, n)
+    gnorm = np.linalg.norm(grad, axis=1)
+    tol_norm, tol_rel = (1e-10, 1e-6) if prec == clbm_lib.FP64 else (1e-6, 5e-4)
+    with sampler(clbm_lib.FP64) as f:
+        for _ in range(3):
+            dirn = rng.normal(0.0, 1.0, base.size)
+            f.load_run(0, S0 + eps * dirn)
+            jp = f.drag_fwd(T, every)
+            f.load_run(0, S0 - eps * dirn)
+            jm = f.drag_fwd(T, every)
+            fd = (jp - jm) / (2 * eps)
+            dn = np.linalg.norm(dirn.reshape(nc, n), axis=1)
+            ad = (grad * dirn.reshape(nc, n)).sum(axis=1)
+            assert (np.abs(ad - fd) / (gnorm * dn) < tol_norm).all(), (ad, fd)
+            well = np.abs(fd) >= 0.1 * gnorm * dn / np.sqrt(n)
+            assert (np.abs(ad - fd)[well] / np.abs(fd)[well] < tol_rel).all(), (ad, fd)
