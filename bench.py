@@ -486,6 +486,9 @@ def main():
     peak, peak_kind = hbm_peak()
     if wl.precision == clbm.FP32:
         kinds = [clbm.describe_variant(int(v)) for v in s.run_variants()]
+        for r, k in enumerate(kinds):  # rows per CTA of each cluster-resident run
+            if k["kind"] == "cluster-resident":
+                k["band_rows"] = [int(x) for x in s.band_rows(r)]
     else:
         kinds = [{"kind": "streaming", "kernel": "k_step_f64", "variant": 0}] * len(wl.runs)
     n_cluster = sum(k["kind"] == "cluster-resident" for k in kinds)

@@ -33,7 +33,7 @@ EXPORTS = [
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
-    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_profile_read_fields", "clbm_autotune", "clbm_set_step_variant", "clbm_set_run_variants", "clbm_get_run_variants", "clbm_shard_plan", "clbm_ref_random_field",
+    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_profile_read_fields", "clbm_autotune", "clbm_set_step_variant", "clbm_set_run_variants", "clbm_get_run_variants", "clbm_band_rows", "clbm_set_band_rows", "clbm_get_band_rows", "clbm_shard_plan", "clbm_ref_random_field",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -111,6 +111,9 @@ def lib() -> C.CDLL:
         L.clbm_set_step_variant.argtypes = [vp, i]
         L.clbm_set_run_variants.argtypes = [vp, vp]
         L.clbm_get_run_variants.argtypes = [vp, vp]
+        L.clbm_band_rows.argtypes = [C.POINTER(RunDesc), i, d, vp]
+        L.clbm_set_band_rows.argtypes = [vp, i, vp, i]
+        L.clbm_get_band_rows.argtypes = [vp, i, vp, C.POINTER(i)]
         L.clbm_profile_read.argtypes = [vp, C.POINTER(d), C.POINTER(i)]
         L.clbm_profile_read_fields.argtypes = [vp, C.POINTER(d), C.POINTER(i)]
         L.clbm_error_word.argtypes = [vp, C.POINTER(C.c_uint), i]
@@ -211,6 +214,15 @@ def shard_plan(labels: np.ndarray, nshards: int, shard: int) -> dict:
 # thread counts 1024, 512, 256 (one launch per run per interval).
 STREAM_VARIANTS = 8
 TEMPORAL_THREADS = (1024, 512, 256)
+CLUSTER_SIZES = (1, 2, 4, 8, 16, 3, 5, 6, 7)  # the autotuner's numbering order
+
+
+def band_rows(run: RunDesc, cluster_size: int, gamma: float) -> np.ndarray:
+    """The band split of a lattice over a cluster balanced for weight gamma
+    (host-only: no device needed)."""
+    a = np.zeros(cluster_size, np.int32)
+    check(lib().clbm_band_rows(C.byref(run), cluster_size, gamma, _p(a)), "clbm_band_rows")
+    return a
 
 
 def describe_variant(v: int) -> dict:
@@ -218,7 +230,7 @@ def describe_variant(v: int) -> dict:
         return {"kind": "streaming", "kernel": "k_step_f32", "variant": v}
     q = v - STREAM_VARIANTS
     return {"kind": "cluster-resident", "kernel": "k_temporal_f32", "variant": v,
-            "cluster_size": 1 << (q // len(TEMPORAL_THREADS)),
+            "cluster_size": CLUSTER_SIZES[q // len(TEMPORAL_THREADS)],
             "threads": TEMPORAL_THREADS[q % len(TEMPORAL_THREADS)]}
 
 
@@ -392,6 +404,17 @@ class Sampler:
         a = np.zeros(len(self.runs), np.int32)
         check(lib().clbm_get_run_variants(self.h, _p(a)), "clbm_get_run_variants")
         return a
+
+    def set_band_rows(self, run: int, rows):
+        a = np.ascontiguousarray(rows, dtype=np.int32)
+        check(lib().clbm_set_band_rows(self.h, run, _p(a) if a.size else None, int(a.size)),
+              "clbm_set_band_rows")
+
+    def band_rows(self, run: int) -> np.ndarray:
+        a = np.zeros(16, np.int32)
+        n = C.c_int()
+        check(lib().clbm_get_band_rows(self.h, run, _p(a), C.byref(n)), "clbm_get_band_rows")
+        return a[:n.value].copy()
 
     def profile(self, enable: bool):
         check(lib().clbm_profile(self.h, int(enable)), "clbm_profile")

@@ -77,6 +77,8 @@ struct clbm_ctx {
   // streaming runs share one step launch per step; every cluster-resident run
   // is one launch per interval on its own side stream, concurrent with them.
   std::vector<int> run_cs, run_tv;
+  // band split of each cluster-resident run (row0[0..cs]; empty = even)
+  std::vector<std::vector<int>> run_rows;
   bool stream_subset = false;       // some runs are cluster-resident: step the rest through...
   RunDev *d_runs_stream = nullptr;  // ...this table (their descriptors, own tile bases)
   std::vector<RunDev> stream_h;
@@ -418,6 +420,7 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
   DevArrays &D = c->d;
   c->run_cs.assign(nruns, 0);
   c->run_tv.assign(nruns, 0);
+  c->run_rows.assign(nruns, std::vector<int>());
   c->stream_nruns = nruns;
   if ((e = dalloc(c->d_runs_stream, nruns)) != cudaSuccess) return bail(e);
   if ((e = dalloc(D.runs, nruns)) != cudaSuccess) return bail(e);
@@ -609,6 +612,7 @@ extern "C" int clbm_init_equilibrium(clbm_ctx *c, int run, double u0, double noi
 // cluster-resident, with which cluster size and thread count.
 struct LbPlan {
   std::vector<int> cs, tv;        // per run: cluster size (0 = streaming), thread variant
+  std::vector<std::vector<int>> rows;  // per run: band split row0[0..cs] (empty = even)
   std::vector<char> active;       // runs to advance (autotuner timing of one run); empty = all
   const RunDev *table = nullptr;  // step-kernel table of the streaming runs
   int nstream = 0, tiles[3] = {0, 0, 0}, variant = 0;
@@ -620,6 +624,7 @@ static LbPlan current_plan(const clbm_ctx *c, bool f64) {
   LbPlan p;
   p.cs = f64 ? std::vector<int>(c->nruns, 0) : c->run_cs;
   p.tv = c->run_tv;
+  p.rows = c->run_rows;
   const bool sub = !f64 && c->stream_subset;
   p.table = sub ? c->d_runs_stream : c->d.runs;
   p.nstream = sub ? c->stream_nruns : c->nruns;
@@ -687,8 +692,13 @@ static cudaError_t enqueue_lb_steps(clbm_ctx *c, const LbPlan &p, int steps, int
     cudaStream_t ts = c->side[i];
     if ((e = cudaStreamWaitEvent(ts, c->fork_join[0], 0)) != cudaSuccess) return e;
     TemporalArgs ta{R, r, steps, (const float *)c->pop[src], (float *)c->pop[dst], (float *)c->d.terms,
-                    c->d.term_slab, c->d.err, c->d_maps};
-    if ((e = launch_temporal(ta, p.cs[r], p.tv[r], R.nclones, R.W, R.H, ts)) != cudaSuccess) return e;
+                    c->d.term_slab, c->d.err, c->d_maps, {}};
+    const int cs = p.cs[r];
+    if (r < (int)p.rows.size() && (int)p.rows[r].size() == cs + 1)
+      std::copy(p.rows[r].begin(), p.rows[r].end(), ta.band_row0);
+    else
+      even_band_rows(R.H, cs, ta.band_row0);
+    if ((e = launch_temporal(ta, cs, p.tv[r], R.nclones, R.W, ts)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(c->fork_join[1 + i], ts)) != cudaSuccess) return e;
     i++;
   }
@@ -707,11 +717,15 @@ static cudaError_t enqueue_lb_steps(clbm_ctx *c, const LbPlan &p, int steps, int
   return cudaSuccess;
 }
 
-// Install a plan: per run cluster size (0 = streaming) and thread variant,
-// the streaming runs' launch variant.  Captured intervals are dropped.
-static cudaError_t set_plan(clbm_ctx *c, const std::vector<int> &cs, const std::vector<int> &tv, int variant) {
+// Install a plan: per run cluster size (0 = streaming), thread variant and
+// band split (empty: even), the streaming runs' launch variant.  Captured
+// intervals are dropped.
+static cudaError_t set_plan(clbm_ctx *c, const std::vector<int> &cs, const std::vector<int> &tv, int variant,
+                            const std::vector<std::vector<int>> &rows = {}) {
   c->run_cs = cs;
   c->run_tv = tv;
+  c->run_rows = rows;
+  c->run_rows.resize(c->nruns);
   c->step_variant = variant;
   std::vector<int> streaming;
   for (int r = 0; r < c->nruns; r++)
@@ -1027,28 +1041,61 @@ extern "C" int clbm_profile_read_fields(clbm_ctx *c, double *field_ms, int *nint
 }
 
 // Variant numbering: 0 .. step_variant_count()-1 are the streaming step
-// launches; after them, for cluster sizes 1, 2, 4, 8, 16 (index log2), the
-// cluster-resident interval kernel's thread configurations.
-static int variant_count() { return step_variant_count() + 5 * temporal_variant_count(); }
+// launches; after them, for each cluster size of kClusterSizes in that order,
+// the cluster-resident interval kernel's thread configurations.  The sizes
+// that are not powers of two come last, so the numbers of the others do not
+// move.  A cluster of 4 fills only the GPCs whose SM count is a multiple of
+// 4 (36 resident clusters of 4 = 144 of GB300's 152 SMs); 3, 5, 6 and 7 pack
+// the GPCs differently and change the rows per band.
+static const int kClusterSizes[] = {1, 2, 4, 8, 16, 3, 5, 6, 7};
+static constexpr int kNumClusterSizes = (int)(sizeof(kClusterSizes) / sizeof(kClusterSizes[0]));
+
+static int variant_count() { return step_variant_count() + kNumClusterSizes * temporal_variant_count(); }
 
 static void variant_shape(int v, int &cs, int &tv) {
   const int nv = step_variant_count();
   cs = 0;
   tv = 0;
-  if (v >= nv) {
+  if (v >= nv && v < variant_count()) {
     const int q = v - nv;
-    cs = 1 << (q / temporal_variant_count());
+    cs = kClusterSizes[q / temporal_variant_count()];
     tv = q % temporal_variant_count();
   }
 }
 
 static int variant_index(int cs, int tv) {
-  return cs ? step_variant_count() + (31 - __builtin_clz((unsigned)cs)) * temporal_variant_count() + tv : 0;
+  for (int j = 0; cs && j < kNumClusterSizes; j++)
+    if (kClusterSizes[j] == cs) return step_variant_count() + j * temporal_variant_count() + tv;
+  return 0;
 }
 
-// whether run r's lattice can run cluster-resident at this shape
+// whether run r's lattice can run cluster-resident at this shape (even split)
 static bool shape_fits(const RunDev &R, int cs, int tv) {
-  return R.H >= cs && temporal_max_clusters(cs, tv, R.W, R.H, R.field_mode != 0) >= 1;
+  return R.H >= cs && cs <= MAX_CLUSTER &&
+         temporal_max_clusters(cs, tv, R.W, (R.H + cs - 1) / cs, R.field_mode != 0) >= 1;
+}
+
+// largest band of a split row0[0..cs]
+static int split_rows_max(const std::vector<int> &row0) {
+  int m = 0;
+  for (size_t b = 0; b + 1 < row0.size(); b++) m = std::max(m, row0[b + 1] - row0[b]);
+  return m;
+}
+
+// Weights of the general path the autotuner balances band splits for.
+static const double kBalanceGamma[] = {0.5, 1.0, 1.5, 2.0, 3.0, 4.0, 6.0, 8.0};
+
+// Run R's band split at cluster size cs balanced for weight gamma, if it
+// differs from the even split and the shape stays resident at thread
+// variant tv; else empty.
+static std::vector<int> balanced_split(const RunDev &R, int cs, int tv, double gamma) {
+  std::vector<int> even(cs + 1), row0(cs + 1);
+  even_band_rows(R.H, cs, even.data());
+  if (!balanced_band_rows(R.W, R.H, R.xmin, R.xmax, R.ymin, R.ymax, cs, gamma, temporal_rows_limit(R.W),
+                          row0.data()) ||
+      row0 == even || temporal_max_clusters(cs, tv, R.W, split_rows_max(row0), R.field_mode != 0) < 1)
+    return {};
+  return row0;
 }
 
 // one variant for every run
@@ -1113,6 +1160,7 @@ struct TuneResult {
   int best;
   std::vector<int> cs, tv;
   int sv;
+  std::vector<std::vector<int>> rows;
 };
 static std::mutex g_tune_mutex;
 static std::map<std::vector<long long>, TuneResult> g_tune_cache;
@@ -1136,7 +1184,7 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
-      CK(set_plan(c, it->second.cs, it->second.tv, it->second.sv));
+      CK(set_plan(c, it->second.cs, it->second.tv, it->second.sv, it->second.rows));
       if (best) *best = it->second.best;
       return CLBM_OK;
     }
@@ -1169,10 +1217,12 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
   best_ms = best_stream_ms;
   arg = best_sv;
   std::vector<int> plan_cs(R, 0), plan_tv(R, 0);
+  std::vector<std::vector<int>> plan_rows(R);
+  std::vector<std::pair<double, int>> shapes;  // (ms per step, variant) of the cluster-resident shapes
   // uniform cluster-resident shapes, timed per step over a full-length
   // interval (their HBM load and store are amortised over the steps)
   const int tsteps = std::min(c->max_steps, 100);
-  for (int cs = 1; cs <= 16; cs *= 2) {
+  for (const int cs : kClusterSizes) {
     for (int tv = 0; tv < ntv; tv++) {
       const int vidx = variant_index(cs, tv);
       if (ms_per_variant) ms_per_variant[vidx] = -1.0;
@@ -1188,6 +1238,7 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
         continue;
       }
       if (ms_per_variant) ms_per_variant[vidx] = per;
+      shapes.emplace_back(per, vidx);
       if (per < best_ms) {
         best_ms = per;
         arg = vidx;
@@ -1196,9 +1247,41 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
       }
     }
   }
+  // balanced band splits of the fastest cluster-resident shapes (up to three,
+  // within 25 % of the fastest): the band holding the square's box, and the
+  // wall bands, carry more work per row than the others, and every step waits
+  // for the slowest band
+  std::sort(shapes.begin(), shapes.end());
+  for (size_t q = 0; q < shapes.size() && q < 3 && shapes[q].first <= 1.25 * shapes[0].first; q++) {
+    int cs, tv;
+    variant_shape(shapes[q].second, cs, tv);
+    for (double g : kBalanceGamma) {
+      std::vector<std::vector<int>> rows(R);
+      bool any = false;
+      for (int r = 0; r < R; r++) {
+        rows[r] = balanced_split(c->runs_h[r], cs, tv, g);
+        any = any || !rows[r].empty();
+      }
+      if (!any) continue;
+      LbPlan p;
+      cudaError_t e = full_plan(c, std::vector<int>(R, cs), std::vector<int>(R, tv), best_sv, p);
+      p.rows = rows;
+      double per = 0.0;
+      if (e == cudaSuccess) e = time_plan(c, p, tsteps, e0, e1, &per);
+      if (e != cudaSuccess) return bail(e);
+      if (per < best_ms) {
+        best_ms = per;
+        arg = shapes[q].second;
+        plan_cs.assign(R, cs);
+        plan_tv.assign(R, tv);
+        plan_rows = rows;
+      }
+    }
+  }
   // per-run plan
   if (R > 1) {
     std::vector<int> pcs(R, 0), ptv(R, 0);
+    std::vector<std::vector<int>> prows(R);
     bool any = false, mixed = false;
     for (int r = 0; r < R; r++) {
       LbPlan p;
@@ -1215,7 +1298,7 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
       if (e == cudaSuccess) e = time_plan(c, p, tsteps, e0, e1, &run_best);
       if (e != cudaSuccess) return bail(e);
       p.nstream = 0;
-      for (int cs = 1; cs <= 16; cs *= 2)
+      for (const int cs : kClusterSizes)
         for (int tv = 0; tv < ntv; tv++) {
           if (!shape_fits(c->runs_h[r], cs, tv)) continue;
           p.cs[r] = cs;
@@ -1231,12 +1314,30 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
             ptv[r] = tv;
           }
         }
+      if (pcs[r] > 0) {  // the run's own best shape, balanced
+        p.cs[r] = pcs[r];
+        p.tv[r] = ptv[r];
+        p.rows.assign(R, std::vector<int>());
+        for (double g : kBalanceGamma) {
+          std::vector<int> row0 = balanced_split(c->runs_h[r], pcs[r], ptv[r], g);
+          if (row0.empty() || row0 == p.rows[r]) continue;
+          p.rows[r] = row0;
+          double per = 0.0;
+          const cudaError_t te = time_plan(c, p, tsteps, e0, e1, &per);
+          if (te != cudaSuccess) return bail(te);
+          if (per < run_best) {
+            run_best = per;
+            prows[r] = row0;
+          }
+        }
+      }
       any = any || pcs[r] > 0;
     }
     for (int r = 0; r < R; r++) mixed = mixed || pcs[r] != pcs[0] || ptv[r] != ptv[0];
     if (any && mixed) {
       LbPlan p;
       cudaError_t e = full_plan(c, pcs, ptv, best_sv, p);
+      p.rows = prows;
       double per = 0.0;
       if (e == cudaSuccess) e = time_plan(c, p, tsteps, e0, e1, &per);
       if (e != cudaSuccess) return bail(e);
@@ -1245,15 +1346,16 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
         arg = CLBM_VARIANT_PER_RUN;
         plan_cs = pcs;
         plan_tv = ptv;
+        plan_rows = prows;
       }
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  CK(set_plan(c, plan_cs, plan_tv, best_sv));
+  CK(set_plan(c, plan_cs, plan_tv, best_sv, plan_rows));
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
-    g_tune_cache[key] = TuneResult{arg, plan_cs, plan_tv, best_sv};
+    g_tune_cache[key] = TuneResult{arg, plan_cs, plan_tv, best_sv, plan_rows};
   }
   if (best) *best = arg;
   return CLBM_OK;
@@ -1291,6 +1393,57 @@ extern "C" int clbm_set_run_variants(clbm_ctx *c, const int *variants) {
     }
   }
   CK(set_plan(c, cs, tv, sv >= 0 ? sv : c->step_variant));
+  return CLBM_OK;
+}
+
+extern "C" int clbm_band_rows(const clbm_run_desc *run, int cluster_size, double gamma, int *rows) {
+  if (!run || !rows) return fail(CLBM_ERR_INVALID, "NULL argument");
+  if (cluster_size < 1 || cluster_size > MAX_CLUSTER || cluster_size > run->height)
+    return fail(CLBM_ERR_INVALID, "cluster size out of range");
+  std::vector<int> row0(cluster_size + 1);
+  if (!balanced_band_rows(run->width, run->height, run->xmin, run->xmax, run->ymin, run->ymax, cluster_size,
+                          gamma, temporal_rows_limit(run->width), row0.data()))
+    return fail(CLBM_ERR_INVALID, "no band split of this lattice fits in shared memory");
+  for (int b = 0; b < cluster_size; b++) rows[b] = row0[b + 1] - row0[b];
+  return CLBM_OK;
+}
+
+extern "C" int clbm_set_band_rows(clbm_ctx *c, int run, const int *rows, int nbands) {
+  if (!c || (!rows && nbands)) return fail(CLBM_ERR_INVALID, "NULL argument");
+  if (run < 0 || run >= c->nruns) return fail(CLBM_ERR_INVALID, "run out of range");
+  const RunDev &R = c->runs_h[run];
+  if (nbands == 0) {  // back to the even split
+    c->run_rows[run].clear();
+    destroy_graphs(c);
+    return CLBM_OK;
+  }
+  if (c->run_cs[run] == 0 || nbands != c->run_cs[run])
+    return fail(CLBM_ERR_INVALID, "nbands must equal the run's cluster size (a cluster-resident variant)");
+  std::vector<int> row0(nbands + 1, 0);
+  for (int b = 0; b < nbands; b++) {
+    if (rows[b] < 1) return fail(CLBM_ERR_INVALID, "every band needs at least one row");
+    row0[b + 1] = row0[b] + rows[b];
+  }
+  if (row0[nbands] != R.H) return fail(CLBM_ERR_INVALID, "band rows must sum to the lattice height");
+  if (temporal_max_clusters(nbands, c->run_tv[run], R.W, split_rows_max(row0), R.field_mode != 0) < 1)
+    return fail(CLBM_ERR_INVALID, "the largest band does not fit in shared memory at this variant");
+  c->run_rows[run] = row0;
+  destroy_graphs(c);
+  return CLBM_OK;
+}
+
+extern "C" int clbm_get_band_rows(clbm_ctx *c, int run, int *rows, int *nbands) {
+  if (!c || !rows || !nbands) return fail(CLBM_ERR_INVALID, "NULL argument");
+  if (run < 0 || run >= c->nruns) return fail(CLBM_ERR_INVALID, "run out of range");
+  const int cs = c->run_cs[run];
+  *nbands = cs;
+  if (!cs) return CLBM_OK;
+  std::vector<int> row0 = c->run_rows[run];
+  if ((int)row0.size() != cs + 1) {
+    row0.assign(cs + 1, 0);
+    even_band_rows(c->runs_h[run].H, cs, row0.data());
+  }
+  for (int b = 0; b < cs; b++) rows[b] = row0[b + 1] - row0[b];
   return CLBM_OK;
 }
 

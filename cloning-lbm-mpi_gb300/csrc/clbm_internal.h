@@ -80,6 +80,9 @@ struct StepArgs {
   const float *maps;  // random body-force fields (nullable)
 };
 
+// largest cluster of the cluster-resident interval kernel (non-portable size)
+constexpr int MAX_CLUSTER = 16;
+
 struct TemporalArgs {
   RunDev rd;          // the run, by value: kernel-parameter space, never aliased
   int run;
@@ -90,6 +93,9 @@ struct TemporalArgs {
   long long term_slab;
   unsigned *err;
   const float *maps;  // random body-force fields (nullable)
+  // band b of a clone (CTA of cluster rank b) holds the lattice rows
+  // [band_row0[b], band_row0[b + 1]); band_row0[cs] = H
+  int band_row0[MAX_CLUSTER + 1];
 };
 
 struct ReseedArgs {
@@ -140,10 +146,21 @@ cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int m
 inline int field_dft_mpad(int W) { return (2 * W + 127) / 128 * 128; }
 inline int field_dft_kchunks(int na) { return (2 * na + 31) / 32; }
 void build_field_dft_image(int W, int M1, const int *alist, int na, int mpad, int kchunks, float *out);
-cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W, int H,
+// cluster-resident interval kernel (clbm_temporal.cu): launch with the bands
+// of a.band_row0; resident clusters of a shape whose largest band has
+// rows_max rows (0: it cannot run); the most rows a band of width W can hold
+cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W,
                             cudaStream_t s);
-int temporal_max_clusters(int cs, int variant, int W, int H, bool field);
+int temporal_max_clusters(int cs, int variant, int W, int rows_max, bool field);
+int temporal_rows_limit(int W);
 int temporal_variant_count();
+// band splits (clbm_bands.cu): row0[0..cs] of H rows in cs bands, the first
+// H % cs one row more; or balanced for an estimated per-step cost in which a
+// node on the general path (walls, the square's box) counts 1 + gamma and a
+// band-edge row 1 + gamma / 4 per node (false: no split within the row limit)
+void even_band_rows(int H, int cs, int *row0);
+bool balanced_band_rows(int W, int H, int xmin, int xmax, int ymin, int ymax, int cs, double gamma,
+                        int rows_limit, int *row0);
 cudaError_t launch_scgf(const double *logr, int first, int count, double dT, double *out,
                         cudaStream_t s);
 cudaError_t launch_init_equilibrium(bool f64, const RunDev *runs, int nruns, int run, void *pop,

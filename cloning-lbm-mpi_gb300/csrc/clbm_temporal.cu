@@ -1,8 +1,9 @@
 // clbm_temporal.cu -- FP32 interval kernel with every clone resident on chip.
 //
 // One thread-block cluster per clone: the clone's H rows are split into CS
-// bands of H/CS rows (the first H % CS bands one more), each band in one
-// CTA's shared memory (nine floats per node, node after node).  The T steps
+// bands of consecutive rows, given by the launch (an even split, or one
+// balanced for the extra cost of the square's rows and the walls), each band
+// in one CTA's shared memory (nine floats per node, node after node).  The T steps
 // of the interval run without touching HBM except for the drag terms: P_0 is
 // loaded once, S_T stored once.
 //
@@ -21,6 +22,8 @@
 // the streaming kernel.  Neighbours across a band edge are read and written
 // in the adjacent CTA's shared memory (distributed shared memory).
 #include <cooperative_groups.h>
+
+#include <algorithm>
 
 #include "clbm_internal.h"
 #include "clbm_physics.cuh"
@@ -220,11 +223,9 @@ __device__ __forceinline__ Band make_band(const TemporalArgs &a, float *A, cg::c
   b.clone = blockIdx.x / b.cs;
   b.W = a.rd.W;
   b.H = a.rd.H;
-  // H rows over cs bands: the first H % cs bands take one row more
-  const int base = b.H / b.cs, extra = b.H % b.cs;
-  b.rows = base + (b.rank < extra ? 1 : 0);
-  b.row0 = b.rank * base + min(b.rank, extra);
-  b.rows_prev = b.rank > 0 ? base + (b.rank - 1 < extra ? 1 : 0) : b.rows;
+  b.row0 = a.band_row0[b.rank];
+  b.rows = a.band_row0[b.rank + 1] - b.row0;
+  b.rows_prev = b.rank > 0 ? b.row0 - a.band_row0[b.rank - 1] : b.rows;
   b.nb = b.rows * b.W;
   b.rowstep = b.W * 9;
   b.prev = b.rank > 0 ? cluster.map_shared_rank(A, b.rank - 1) : A;
@@ -447,8 +448,14 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
 
 typedef void (*TemporalFn)(TemporalArgs);
 
-// rows of the largest band (the first H % cs bands take one row more)
-static int band_rows_max(int H, int cs) { return (H + cs - 1) / cs; }
+// shared memory a CTA may use
+static constexpr size_t kSmemLimit = 227 * 1024;
+
+int temporal_rows_limit(int W) {
+  int r = 0;
+  while (temporal_smem((r + 1) * W) <= kSmemLimit) r++;
+  return r;
+}
 
 struct TemporalVariant {
   int threads;
@@ -462,9 +469,10 @@ static const TemporalVariant kTemporal[] = {{1024, GENERIC(1024, 1)}, {512, GENE
 int temporal_variant_count() { return (int)(sizeof(kTemporal) / sizeof(kTemporal[0])); }
 
 // the kernel of a variant for this band shape, or nullptr when it cannot run it
-static TemporalFn temporal_fn(int variant, int cs, int W, int H, bool field) {
-  if (variant < 0 || variant >= temporal_variant_count() || cs < 1 || H < cs) return nullptr;
-  if (temporal_smem(band_rows_max(H, cs) * W) > 227 * 1024) return nullptr;
+static TemporalFn temporal_fn(int variant, int cs, int W, int rows_max, bool field) {
+  if (variant < 0 || variant >= temporal_variant_count() || cs < 1 || cs > MAX_CLUSTER || rows_max < 1)
+    return nullptr;
+  if (temporal_smem(rows_max * W) > kSmemLimit) return nullptr;
   return kTemporal[variant].fn[field];
 }
 
@@ -490,13 +498,22 @@ static cudaError_t prepare(TemporalFn fn, int cs, size_t smem) {
   return e;
 }
 
-// Launch one run's interval with cluster size cs (cs <= H).
-cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W, int H,
+// Launch one run's interval with cluster size cs over the bands of
+// a.band_row0 (every band at least one row).
+cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclones, int W,
                             cudaStream_t s) {
   const bool field = a.rd.field_mode != 0 && a.maps != nullptr;
-  TemporalFn fn = temporal_fn(variant, cs, W, H, field);
+  if (cs < 1 || cs > MAX_CLUSTER || a.band_row0[0] != 0 || a.band_row0[cs] != a.rd.H)
+    return cudaErrorInvalidConfiguration;
+  int rows_max = 0;
+  for (int b = 0; b < cs; b++) {
+    const int rows = a.band_row0[b + 1] - a.band_row0[b];
+    if (rows < 1) return cudaErrorInvalidConfiguration;
+    rows_max = std::max(rows_max, rows);
+  }
+  TemporalFn fn = temporal_fn(variant, cs, W, rows_max, field);
   if (!fn || a.steps < 1) return cudaErrorInvalidConfiguration;
-  const size_t smem = temporal_smem(band_rows_max(H, cs) * W);
+  const size_t smem = temporal_smem(rows_max * W);
   cudaError_t e = prepare(fn, cs, smem);
   if (e != cudaSuccess) return e;
   cudaLaunchAttribute attr[1];
@@ -505,10 +522,10 @@ cudaError_t launch_temporal(const TemporalArgs &a, int cs, int variant, int nclo
 }
 
 // Whether the cluster shape can be resident at all (occupancy query, no launch).
-int temporal_max_clusters(int cs, int variant, int W, int H, bool field) {
-  TemporalFn fn = temporal_fn(variant, cs, W, H, field);
+int temporal_max_clusters(int cs, int variant, int W, int rows_max, bool field) {
+  TemporalFn fn = temporal_fn(variant, cs, W, rows_max, field);
   if (!fn) return 0;
-  const size_t smem = temporal_smem(band_rows_max(H, cs) * W);
+  const size_t smem = temporal_smem(rows_max * W);
   if (prepare(fn, cs, smem) != cudaSuccess) return 0;
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = temporal_config(cs, variant, 64, smem, nullptr, attr);

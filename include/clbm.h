@@ -281,10 +281,13 @@ int clbm_profile_read_fields(clbm_ctx *ctx, double *field_ms, int *nintervals);
  * variants (block size, registers per thread, store caching; one launch per
  * step), then the cluster-resident interval kernel (every clone's populations
  * in the shared memory of one thread-block cluster for all the steps of an
- * interval, one launch per interval) for cluster sizes 1, 2, 4, 8, 16 and
- * three thread counts (1024, 512, 256), where every lattice fits: at most
- * 8 + 15 uniform variants.  With several runs it then times each run alone on
- * every shape that fits its lattice and, when the runs' own bests differ,
+ * interval, one launch per interval) for cluster sizes 1, 2, 4, 8, 16, 3, 5,
+ * 6, 7 (numbered in that order) and three thread counts (1024, 512, 256),
+ * where every lattice fits: at most 8 + 27 uniform variants.  For the fastest
+ * cluster-resident shapes it then times band splits balanced for the extra
+ * cost of the square's rows and the walls (clbm_band_rows).  With several runs
+ * it then times each run alone on every shape that fits its lattice (and its
+ * best shape balanced) and, when the runs' own bests differ,
  * the per-run plan as a whole: each cluster-resident run is one launch per
  * interval on its own stream, concurrent with one step launch per step of
  * the streaming runs (a CUDA-graph interval holds them as parallel
@@ -305,6 +308,22 @@ int clbm_set_step_variant(clbm_ctx *ctx, int variant);
 int clbm_set_run_variants(clbm_ctx *ctx, const int *variants);
 /* the variant each run uses now (nruns entries) */
 int clbm_get_run_variants(clbm_ctx *ctx, int *variants);
+/* Band split of a cluster-resident run: cluster rank b holds rows[b]
+ * consecutive lattice rows (from the bottom wall up) of every clone.  An even
+ * split (H / cs rows, the first H % cs bands one more) is the default and what
+ * a variant change restores; the autotuner also times splits balanced for the
+ * extra cost of the square's rows and the walls and keeps the fastest.  The
+ * results do not depend on the split (bit-identical).
+ * clbm_band_rows: the split of a lattice balanced for weight gamma (a node on
+ * the general update path counts 1 + gamma; gamma <= 0: the even split), cs
+ * entries, host-only.  clbm_set_band_rows: nbands = the run's cluster size
+ * (a cluster-resident variant must be set), every band at least one row,
+ * rows summing to the height, the largest band within shared memory; nbands 0
+ * restores the even split.  clbm_get_band_rows: *nbands = the run's cluster
+ * size (0 for a streaming run) and that many rows. */
+int clbm_band_rows(const clbm_run_desc *run, int cluster_size, double gamma, int *rows);
+int clbm_set_band_rows(clbm_ctx *ctx, int run, const int *rows, int nbands);
+int clbm_get_band_rows(clbm_ctx *ctx, int run, int *rows, int *nbands);
 
 /* Macroscopic fields of a clone's current pre-collision state, HOST arrays of
  * Dx*Dy values in the reference's node order y + Dy*x: rho, ux (shifted by

@@ -14,8 +14,11 @@ NSTREAM = 8   # streaming launch variants come first in the autotuner's numberin
 NTHREAD = 3   # thread configurations of the cluster-resident kernel (1024, 512, 256)
 
 
+CLUSTER_SIZES = (1, 2, 4, 8, 16, 3, 5, 6, 7)  # the autotuner's order
+
+
 def temporal_variant(cs, tv=0):
-    return NSTREAM + int(np.log2(cs)) * NTHREAD + tv
+    return NSTREAM + CLUSTER_SIZES.index(cs) * NTHREAD + tv
 
 
 @pytest.mark.parametrize("W,H,side,xc,yc,cs,tv,field", [
@@ -32,6 +35,10 @@ def temporal_variant(cs, tv=0):
     (64, 25, 6, 16, 12, 4, 0, False),    # H % cs != 0: bands of 7, 6, 6, 6 rows
     (96, 23, 5, 30, 9, 4, 2, True),      # bands of 6, 6, 6, 5 rows, field
     (200, 50, 8, 50, 25, 8, 1, False),   # bands of 7 and 6 rows, square across bands
+    (64, 25, 6, 16, 12, 3, 0, False),    # cluster sizes that are not powers of two
+    (96, 23, 5, 30, 9, 5, 1, True),
+    (200, 50, 8, 50, 25, 6, 2, False),
+    (64, 32, 6, 20, 16, 7, 1, False),
 ])
 def test_temporal_equals_streaming(gpu, clbm_lib, orc, W, H, side, xc, yc, cs, tv, field):
     g = orc.channel_geom(W, H, side, xc, yc)
@@ -70,7 +77,7 @@ def test_autotune_considers_cluster_resident_kernel(gpu, clbm_lib, orc):
         s.init_equilibrium(0, 0.04, 1e-3, 3)
         before = s.dump(0, 5)
         best, ms = s.autotune(launches=2)
-        assert len(ms) == NSTREAM + 5 * NTHREAD
+        assert len(ms) == NSTREAM + len(CLUSTER_SIZES) * NTHREAD
         assert (ms[NSTREAM:] > 0).any(), ms
         assert np.array_equal(s.dump(0, 5), before)
         s.run_interval(20)
@@ -105,11 +112,13 @@ def test_graph_replay_with_cluster_resident_kernel(gpu, clbm_lib, orc):
             assert np.array_equal(s.dump(0, j), ref_state[j])
 
 
-def test_bench_lattice_at_bench_shape(gpu, clbm_lib, orc):
+@pytest.mark.parametrize("cs,rows", [(4, None), (3, [24, 16, 24])])
+def test_bench_lattice_at_bench_shape(gpu, clbm_lib, orc, cs, rows):
     """The bench's clone lattice (256x64, square 12) at the bench's interval
-    length and the shape the autotuner picks there (cluster size 4, 1024
-    threads): bit-identical to the streaming kernel, and mass conserved
-    (bounce-back and the body force keep sum f; FP32 rounding only)."""
+    length and the shapes the autotuner picks there (cluster size 4, and
+    cluster size 3 with the square's band 16 rows high, 1024 threads):
+    bit-identical to the streaming kernel, and mass conserved (bounce-back and
+    the body force keep sum f; FP32 rounding only)."""
     from clbm import configs
     r = configs.WORKLOADS["c3"]().runs[0]
     g = orc.channel_geom(r.width, r.height, r.side, r.xc, r.yc)
@@ -118,9 +127,12 @@ def test_bench_lattice_at_bench_shape(gpu, clbm_lib, orc):
                          dt=r.dt, perturb_mode=clbm_lib.PERTURB_UNIFORM, eps=1e-3, seed=5)
     T = 100
     out = []
-    for variant in (7, temporal_variant(4, 0)):
+    for variant in (7, temporal_variant(cs, 0)):
         with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T) as s:
             s.set_step_variant(variant)
+            if rows and variant != 7:
+                s.set_band_rows(0, rows)
+                assert list(s.band_rows(0)) == rows
             s.init_equilibrium(0, r.u0, 1e-3, 9)
             m0 = [s.dump(0, j).sum() for j in range(8)]
             s.run_interval(T)
@@ -134,3 +146,57 @@ def test_bench_lattice_at_bench_shape(gpu, clbm_lib, orc):
             out.append(res)
     for a, b in zip(*out):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("W,H,side,xc,yc,cs,tv,rows", [
+    (64, 24, 6, 16, 12, 3, 0, [10, 4, 10]),
+    (64, 24, 6, 16, 12, 4, 1, [1, 11, 11, 1]),       # one-row bands: both neighbours across CTAs
+    (96, 23, 5, 30, 9, 2, 2, [20, 3]),
+    (200, 50, 8, 50, 25, 5, 0, [12, 8, 6, 12, 12]),
+])
+def test_band_split_equals_streaming(gpu, clbm_lib, orc, W, H, side, xc, yc, cs, tv, rows):
+    """Uneven band splits (set through clbm_set_band_rows), in eager and
+    graph-captured intervals: bit-identical to the streaming kernel."""
+    g = orc.channel_geom(W, H, side, xc, yc)
+    u0, nc, T = 0.05, 4, 21
+    d = clbm_lib.RunDesc(width=g.nx, height=g.ny, xmin=g.xmin, xmax=g.xmax, ymin=g.ymin, ymax=g.ymax,
+                         nclones=nc, ranks=1, tau=0.57, beta=side * u0 * u0 / ((W - 1) * (H - 1)), alpha=8.0,
+                         force_scale=2 / (u0 * u0 * side), dt=u0 / side, perturb_mode=clbm_lib.PERTURB_UNIFORM,
+                         eps=1e-4, seed=7)
+    with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T) as s:
+        s.set_step_variant(4)
+        s.init_equilibrium(0, u0, 1e-3, 7)
+        ref = s.run_sampler(T, 3)
+        ref_state = [s.dump(0, j) for j in range(nc)]
+    for flags in (0, clbm_lib.FLAG_GRAPH):
+        with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T, flags=flags) as s:
+            s.set_step_variant(temporal_variant(cs, tv))
+            assert s.band_rows(0).sum() == H and len(s.band_rows(0)) == cs
+            s.set_band_rows(0, rows)
+            assert list(s.band_rows(0)) == rows
+            s.init_equilibrium(0, u0, 1e-3, 7)
+            rv = [s.run_sampler(T, 2)]
+            s.set_band_rows(0, [])  # back to the even split between captured intervals
+            rv.append(s.run_sampler(T, 1))
+            assert s.error_word() == 0
+            assert np.array_equal(np.concatenate(rv, axis=1), ref)
+            for j in range(nc):
+                assert np.array_equal(s.dump(0, j), ref_state[j])
+
+
+def test_band_rows_checks(gpu, clbm_lib, orc):
+    g = orc.channel_geom(64, 24, 6, 16, 12)
+    d = clbm_lib.RunDesc(width=g.nx, height=g.ny, xmin=g.xmin, xmax=g.xmax, ymin=g.ymin, ymax=g.ymax,
+                         nclones=2, ranks=1, tau=0.57, beta=1e-6, alpha=1.0, force_scale=1.0, dt=0.01)
+    with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=10) as s:
+        s.set_step_variant(4)
+        assert len(s.band_rows(0)) == 0  # streaming run: no bands
+        with pytest.raises(clbm_lib.ClbmError):  # not cluster-resident
+            s.set_band_rows(0, [12, 12])
+        s.set_step_variant(temporal_variant(2, 0))
+        for bad in ([12, 11], [24, 0], [8, 8, 8], [25, -1]):
+            with pytest.raises(clbm_lib.ClbmError):
+                s.set_band_rows(0, bad)
+        s.set_band_rows(0, [5, 19])
+        s.set_step_variant(temporal_variant(2, 0))  # a variant change restores the even split
+        assert list(s.band_rows(0)) == [12, 12]
