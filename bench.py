@@ -416,6 +416,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 run of the same workload")
     ap.add_argument("--variant", type=int, default=None,
                     help="use this interval kernel variant instead of autotuning (profiling)")
+    ap.add_argument("--band-rows", default=None,
+                    help="with --variant: rows per CTA of the cluster-resident kernel, e.g. 24,16,24 (profiling)")
     ap.add_argument("--study", choices=["precision", "adjoint", "drag"], default=None)
     ap.add_argument("--drag", choices=["stress", "momentum"], default="stress",
                     help="drag estimator of the weights (stress: the reference's)")
@@ -453,6 +455,9 @@ def main():
         best, tune_ms = s.autotune(launches=5)
     else:
         s.set_step_variant(args.variant)
+        if args.band_rows:
+            for i in range(len(wl.runs)):
+                s.set_band_rows(i, [int(x) for x in args.band_rows.split(",")])
         best, tune_ms = args.variant, []
     s.run_sampler(wl.steps, 1)
     s.sync()

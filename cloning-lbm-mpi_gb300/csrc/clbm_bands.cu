@@ -23,12 +23,13 @@ void even_band_rows(int H, int cs, int *row0) {
 }
 
 // Per-step cost of row y in node units: W, plus gamma per node on the
-// general path -- a wall row entirely, a row of the square's box the 32-node
-// segments (row-aligned) that touch the box.
+// general path (in a row of the square's box, the 32-node segments,
+// row-aligned, that touch the box) and gamma / 4 per node of a wall row
+// (bounce-back built into the bulk update).
 static double row_cost(int W, int H, int xmin, int xmax, int ymin, int ymax, int y, double gamma) {
   double g = 0.0;
   if (y == 0 || y == H - 1) {
-    g = W;
+    g = 0.25 * W;
   } else if (y >= ymin && y <= ymax) {
     const int x0 = std::max(0, xmin) / 32 * 32;
     const int x1 = std::min(W, (std::min(W - 1, xmax) / 32 + 1) * 32);

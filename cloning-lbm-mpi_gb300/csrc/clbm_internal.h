@@ -156,8 +156,8 @@ int temporal_rows_limit(int W);
 int temporal_variant_count();
 // band splits (clbm_bands.cu): row0[0..cs] of H rows in cs bands, the first
 // H % cs one row more; or balanced for an estimated per-step cost in which a
-// node on the general path (walls, the square's box) counts 1 + gamma and a
-// band-edge row 1 + gamma / 4 per node (false: no split within the row limit)
+// node on the general path (the square's box) counts 1 + gamma and a node of
+// a wall or band-edge row 1 + gamma / 4 (false: no split within the row limit)
 void even_band_rows(int H, int cs, int *row0);
 bool balanced_band_rows(int W, int H, int xmin, int xmax, int ymin, int ymax, int cs, double gamma,
                         int rows_limit, int *row0);

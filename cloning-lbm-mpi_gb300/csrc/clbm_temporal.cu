@@ -251,14 +251,17 @@ __device__ __forceinline__ void load_band(const Band &b, float *A) {
   }
 }
 
-// One node away from the walls and the square, not the last step of the
-// interval.  C, U, D = the node's row and the rows above (y-1) and below
-// (y+1); om, o0, op = the column offsets of x-1, x, x+1 (times 9).  GATHER:
-// S(n,k) = A[n - c_k][opp k], P(n,k) -> A[n + c_k][k]; local step: S(n,k) =
-// A[n][k], P(n,k) -> A[n][opp k].  FIELD: beta scaled by (1 + feps * map[0]),
-// feps = 0 once the field's steps are over (field_beta_f32 then returns beta
-// exactly).  A density at or below zero sets `bad`.
-template <bool GATHER, bool FIELD>
+// One node away from the square, not the last step of the interval.  C, U,
+// D = the node's row and the rows above (y-1) and below (y+1); om, o0, op =
+// the column offsets of x-1, x, x+1 (times 9).  GATHER: S(n,k) = A[n -
+// c_k][opp k], P(n,k) -> A[n + c_k][k]; local step: S(n,k) = A[n][k], P(n,k)
+// -> A[n][opp k].  WALL (gather step): 1 = the bottom wall y = 0, whose
+// slots 2, 5, 6 bounce back (S(n,k) = A[n][k], and P(n, opp k) returns
+// there); 2 = the top wall y = H - 1, slots 4, 7, 8; the row beyond the wall
+// is not touched.  FIELD: beta scaled by (1 + feps * map[0]), feps = 0 once
+// the field's steps are over (field_beta_f32 then returns beta exactly).  A
+// density at or below zero sets `bad`.
+template <bool GATHER, bool FIELD, int WALL = 0>
 __device__ __forceinline__ void update_fast(const RunDev &R, float *C, float *U, float *D, int om, int o0,
                                             int op, const float *map, float feps, bool &bad) {
   float S[9];
@@ -266,12 +269,12 @@ __device__ __forceinline__ void update_fast(const RunDev &R, float *C, float *U,
     S[0] = C[o0 + 0];
     S[1] = C[om + 3];
     S[3] = C[op + 1];
-    S[2] = U[o0 + 4];
-    S[5] = U[om + 7];
-    S[6] = U[op + 8];
-    S[4] = D[o0 + 2];
-    S[7] = D[op + 5];
-    S[8] = D[om + 6];
+    S[2] = WALL == 1 ? C[o0 + 2] : U[o0 + 4];
+    S[5] = WALL == 1 ? C[o0 + 5] : U[om + 7];
+    S[6] = WALL == 1 ? C[o0 + 6] : U[op + 8];
+    S[4] = WALL == 2 ? C[o0 + 4] : D[o0 + 2];
+    S[7] = WALL == 2 ? C[o0 + 7] : D[op + 5];
+    S[8] = WALL == 2 ? C[o0 + 8] : D[om + 6];
   } else {
 #pragma unroll
     for (int k = 0; k < 9; k++) S[k] = C[o0 + k];
@@ -283,15 +286,78 @@ __device__ __forceinline__ void update_fast(const RunDev &R, float *C, float *U,
     C[o0 + 0] = P[0];
     C[op + 1] = P[1];
     C[om + 3] = P[3];
-    D[o0 + 2] = P[2];
-    D[op + 5] = P[5];
-    D[om + 6] = P[6];
-    U[o0 + 4] = P[4];
-    U[om + 7] = P[7];
-    U[op + 8] = P[8];
+    if (WALL == 2) {
+      C[o0 + 4] = P[2];
+      C[o0 + 7] = P[5];
+      C[o0 + 8] = P[6];
+    } else {
+      D[o0 + 2] = P[2];
+      D[op + 5] = P[5];
+      D[om + 6] = P[6];
+    }
+    if (WALL == 1) {
+      C[o0 + 2] = P[4];
+      C[o0 + 5] = P[7];
+      C[o0 + 6] = P[8];
+    } else {
+      U[o0 + 4] = P[4];
+      U[om + 7] = P[7];
+      U[op + 8] = P[8];
+    }
   } else {
 #pragma unroll
     for (int k = 0; k < 9; k++) C[o0 + opp_of(k)] = P[k];
+  }
+}
+
+// A gather step of one node of a band-edge row (the band holds at least two
+// rows): UP, the row above (y - 1) is the previous CTA's last row; else the
+// row below (y + 1) is the next CTA's first row.  The remote row's slots are
+// read and written at 32-bit shared::cluster addresses (Rc = that row's
+// column 0), the node's own row C and the other neighbour row L in this CTA's
+// shared memory; same slots and arithmetic as update_fast.
+template <bool FIELD, bool UP>
+__device__ __forceinline__ void update_edge(const RunDev &R, float *C, float *L, unsigned Rc, int om, int o0,
+                                            int op, const float *map, float feps, bool &bad) {
+  float S[9];
+  S[0] = C[o0 + 0];
+  S[1] = C[om + 3];
+  S[3] = C[op + 1];
+  if (UP) {
+    S[4] = L[o0 + 2];
+    S[7] = L[op + 5];
+    S[8] = L[om + 6];
+    S[2] = ld_cluster(Rc + 4u * (o0 + 4));
+    S[5] = ld_cluster(Rc + 4u * (om + 7));
+    S[6] = ld_cluster(Rc + 4u * (op + 8));
+  } else {
+    S[2] = L[o0 + 4];
+    S[5] = L[om + 7];
+    S[6] = L[op + 8];
+    S[4] = ld_cluster(Rc + 4u * (o0 + 2));
+    S[7] = ld_cluster(Rc + 4u * (op + 5));
+    S[8] = ld_cluster(Rc + 4u * (om + 6));
+  }
+  float P[9];
+  const float drho = collide_f32_run(R, S, P, FIELD ? map : nullptr, feps);
+  bad |= !(drho > -1.0f);
+  C[o0 + 0] = P[0];
+  C[op + 1] = P[1];
+  C[om + 3] = P[3];
+  if (UP) {
+    L[o0 + 2] = P[2];
+    L[op + 5] = P[5];
+    L[om + 6] = P[6];
+    st_cluster(Rc + 4u * (o0 + 4), P[4]);
+    st_cluster(Rc + 4u * (om + 7), P[7]);
+    st_cluster(Rc + 4u * (op + 8), P[8]);
+  } else {
+    L[o0 + 4] = P[4];
+    L[om + 7] = P[7];
+    L[op + 8] = P[8];
+    st_cluster(Rc + 4u * (o0 + 2), P[2]);
+    st_cluster(Rc + 4u * (op + 5), P[5]);
+    st_cluster(Rc + 4u * (om + 6), P[6]);
   }
 }
 
@@ -300,23 +366,28 @@ __device__ __forceinline__ float field_eps(const TemporalArgs &a, int t) {
 }
 
 // Shared memory of one CTA: the band's populations, then the segment list,
-// one class byte per 32-node segment and the three range ends of the list.
+// one class byte per 32-node segment and the five range ends of the list.
 __host__ __device__ inline size_t temporal_smem(int nb) {
   const int nseg = (nb + 31) / 32;
-  return sizeof(float) * 9 * (size_t)nb + 2 * (size_t)((nseg + 7) & ~7) + (size_t)((nseg + 15) & ~15) + 16;
+  return sizeof(float) * 9 * (size_t)nb + 2 * (size_t)((nseg + 7) & ~7) + (size_t)((nseg + 15) & ~15) + 32;
 }
 
 // One step of every segment of the band (all but the interval's last step).
-// The list holds the segments by class: the square's box and the walls (and
-// a partial last segment) first, then the band-edge rows, the bulk segments
-// with the periodic wrap and the interior bulk segments; entry k belongs to
-// warp k % NW in every range.  Gather step: the first range through the
-// general path, band-edge rows through its plain form (no bounce-back, the
-// neighbour rows through distributed shared memory), wrap segments with
-// per-node column offsets, interior segments with their nine slots at
-// constant offsets from the node's own (-9 / +9 floats for x -+ 1, -+ rowstep
-// for y -+ 1).  Local step: a node touches only its own nine slots, so only
-// the first range (the box: drag terms, the interior) needs the general path.
+// The list holds the segments by class, in this order: the square's box (and
+// a partial last segment, and wall or band-edge segments that span two rows
+// at a wall), the wall rows, the band-edge rows, other segments spanning two
+// rows at a band edge, the bulk segments with the periodic wrap and the
+// interior bulk segments; range[c] = the end of the c-th range, and entry k
+// of every range belongs to warp k % NW.  Gather step: the box range through
+// the general path; wall rows through update_fast with the wall's bounce-back
+// built in; band-edge rows with the neighbour row across the band edge at
+// shared::cluster addresses and the rest in this CTA; rows spanning a band
+// edge through the plain form of the general path (no bounce-back, every
+// slot at a shared::cluster address); wrap segments with per-node column
+// offsets; interior segments with their nine slots at constant offsets from
+// the node's own (-9 / +9 floats for x -+ 1, -+ rowstep for y -+ 1).  Local
+// step: a node touches only its own nine slots, so only the box range (drag
+// terms, the interior) needs the general path.
 template <int NW, bool GATHER, bool FIELD>
 __device__ __forceinline__ void band_step(const TemporalArgs &a, const Band &b, float *A,
                                           const unsigned short *list, int nseg, const int *range,
@@ -341,20 +412,42 @@ __device__ __forceinline__ void band_step(const TemporalArgs &a, const Band &b, 
     }
     return;
   }
-  const int nedge = range[1], nwrap = range[2];
-  for (int k = ngen + ((warp - ngen) & (NW - 1)); k < nedge; k += NW)
-    update_general_gather<true>(a, b, list[k] * 32 + lane, t, bad, terms);
-  for (int k = nedge + ((warp - nedge) & (NW - 1)); k < nwrap; k += NW) {
+  const int rs = b.rowstep;
+  const int nwall = range[1], nedge = range[2], nspan = range[3], nwrap = range[4];
+  for (int k = ngen + ((warp - ngen) & (NW - 1)); k < nwall; k += NW) {
     const int i = list[k] * 32 + lane;
     const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
     const int o0 = x * 9, om = (x == 0 ? b.W - 1 : x - 1) * 9, op = (x == b.W - 1 ? 0 : x + 1) * 9;
-    float *C = A + ly * b.rowstep;
-    update_fast<true, FIELD>(R, C, C - b.rowstep, C + b.rowstep, om, o0, op, map + i, feps, bad);
+    float *C = A + ly * rs;
+    if (b.row0 + ly == 0)  // warp-uniform: a wall segment lies in one row
+      update_fast<true, FIELD, 1>(R, C, C - rs, C + rs, om, o0, op, map + i, feps, bad);
+    else
+      update_fast<true, FIELD, 2>(R, C, C - rs, C + rs, om, o0, op, map + i, feps, bad);
+  }
+  for (int k = nwall + ((warp - nwall) & (NW - 1)); k < nedge; k += NW) {
+    const int i = list[k] * 32 + lane;
+    const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
+    const int o0 = x * 9, om = (x == 0 ? b.W - 1 : x - 1) * 9, op = (x == b.W - 1 ? 0 : x + 1) * 9;
+    float *C = A + ly * rs;
+    if (ly == 0)  // warp-uniform: an edge segment lies in one row
+      update_edge<FIELD, true>(R, C, C + rs, b.prev_c + 4u * (unsigned)((b.rows_prev - 1) * rs), om, o0, op,
+                               map + i, feps, bad);
+    else
+      update_edge<FIELD, false>(R, C, C - rs, b.next_c, om, o0, op, map + i, feps, bad);
+  }
+  for (int k = nedge + ((warp - nedge) & (NW - 1)); k < nspan; k += NW)
+    update_general_gather<true>(a, b, list[k] * 32 + lane, t, bad, terms);
+  for (int k = nspan + ((warp - nspan) & (NW - 1)); k < nwrap; k += NW) {
+    const int i = list[k] * 32 + lane;
+    const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W;
+    const int o0 = x * 9, om = (x == 0 ? b.W - 1 : x - 1) * 9, op = (x == b.W - 1 ? 0 : x + 1) * 9;
+    float *C = A + ly * rs;
+    update_fast<true, FIELD>(R, C, C - rs, C + rs, om, o0, op, map + i, feps, bad);
   }
   for (int k = nwrap + ((warp - nwrap) & (NW - 1)); k < nseg; k += NW) {
     const int i = list[k] * 32 + lane;
     float *C = A + i * 9;
-    update_fast<true, FIELD>(R, C, C - b.rowstep, C + b.rowstep, -9, 0, 9, map + i, feps, bad);
+    update_fast<true, FIELD>(R, C, C - rs, C + rs, -9, 0, 9, map + i, feps, bad);
   }
 }
 
@@ -384,37 +477,50 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
   unsigned char *cls = (unsigned char *)(list + ((nseg + 7) & ~7));
   int *count_s = (int *)(cls + ((nseg + 15) & ~15));
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  // segment classes: 4 touches the square's box, 3 a wall row or past the
-  // band's end (partial last segment), 2 a band-edge row (neighbour row in
-  // another CTA), 1 bulk with the periodic wrap, 0 interior bulk
+  // segment classes: 5 touches the square's box, or past the band's end
+  // (partial last segment), or a wall row that is not alone in its segment or
+  // in its band; 4 a wall row (its neighbour row in this CTA); 3 a band-edge
+  // row (neighbour row in another CTA, the other in this one); 2 other
+  // segments touching a band-edge row (spanning two rows, or a one-row band);
+  // 1 bulk with the periodic wrap; 0 interior bulk
   for (int sg = warp; sg < nseg; sg += NW) {
     const int i = sg * 32 + lane;
     const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W, y = b.row0 + ly;
     const bool pad = i >= b.nb;
     const bool box = !pad && x >= R.xmin && x <= R.xmax && y >= R.ymin && y <= R.ymax;
-    const bool wall = pad || y == 0 || y == b.H - 1;
+    const bool wall = !pad && (y == 0 || y == b.H - 1);
     const bool edge = !pad && b.cs > 1 && (ly == 0 || ly == b.rows - 1);
+    // (every lane takes part in the shuffle: it is not under the && below)
+    const int ly0 = __shfl_sync(0xffffffffu, ly, 0);
+    const bool one_row = __all_sync(0xffffffffu, !pad && ly == ly0) && b.rows > 1;
     const bool inner = __all_sync(0xffffffffu, !pad && x > 0 && x < b.W - 1);
-    const int c = __any_sync(0xffffffffu, box) ? 4 : __any_sync(0xffffffffu, wall) ? 3
-                  : __any_sync(0xffffffffu, edge) ? 2 : inner ? 0 : 1;
+    int c;
+    if (__any_sync(0xffffffffu, box || pad))
+      c = 5;
+    else if (__any_sync(0xffffffffu, wall))
+      c = one_row ? 4 : 5;
+    else if (__any_sync(0xffffffffu, edge))
+      c = one_row ? 3 : 2;
+    else
+      c = inner ? 0 : 1;
     if (lane == 0) cls[sg] = (unsigned char)c;
   }
   __syncthreads();
-  if (warp == 0) {  // the list, class 4 first; range ends after classes 3, 2, 1
+  if (warp == 0) {  // the list, class 5 first; range ends after classes 5, 4, 3, 2, 1
     const unsigned lower = (1u << lane) - 1u;
     int n = 0;
-    for (int pass = 4; pass >= 0; pass--) {
+    for (int pass = 5; pass >= 0; pass--) {
       for (int c = 0; c < nseg; c += 32) {
         const bool take = c + lane < nseg && cls[c + lane] == pass;
         const unsigned m = __ballot_sync(0xffffffffu, take);
         if (take) list[n + __popc(m & lower)] = (unsigned short)(c + lane);
         n += __popc(m);
       }
-      if (lane == 0 && pass >= 1 && pass <= 3) count_s[3 - pass] = n;
+      if (lane == 0 && pass >= 1) count_s[5 - pass] = n;
     }
   }
   __syncthreads();
-  const int range[3] = {count_s[0], count_s[1], count_s[2]};
+  const int range[5] = {count_s[0], count_s[1], count_s[2], count_s[3], count_s[4]};
   const float *map = FIELD ? a.maps + R.map_base + (long long)b.clone * R.nodes + (long long)b.row0 * b.W : nullptr;
   bool bad = false;
   cluster.sync();

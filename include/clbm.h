@@ -315,7 +315,8 @@ int clbm_get_run_variants(clbm_ctx *ctx, int *variants);
  * extra cost of the square's rows and the walls and keeps the fastest.  The
  * results do not depend on the split (bit-identical).
  * clbm_band_rows: the split of a lattice balanced for weight gamma (a node on
- * the general update path counts 1 + gamma; gamma <= 0: the even split), cs
+ * the general update path, the square's box, counts 1 + gamma, a node of a
+ * wall or band-edge row 1 + gamma / 4; gamma <= 0: the even split), cs
  * entries, host-only.  clbm_set_band_rows: nbands = the run's cluster size
  * (a cluster-resident variant must be set), every band at least one row,
  * rows summing to the height, the largest band within shared memory; nbands 0

@@ -11,7 +11,7 @@ SMEM_LIMIT = 227 * 1024
 
 def smem(nb):
     nseg = (nb + 31) // 32
-    return 36 * nb + 2 * ((nseg + 7) & ~7) + ((nseg + 15) & ~15) + 16
+    return 36 * nb + 2 * ((nseg + 7) & ~7) + ((nseg + 15) & ~15) + 32
 
 
 def rows_limit(W):
@@ -24,7 +24,7 @@ def rows_limit(W):
 def row_cost(W, H, xmin, xmax, ymin, ymax, y, g):
     gen = 0
     if y in (0, H - 1):
-        gen = W
+        gen = 0.25 * W
     elif ymin <= y <= ymax:
         x0 = max(0, xmin) // 32 * 32
         x1 = min(W, (min(W - 1, xmax) // 32 + 1) * 32)
@@ -60,7 +60,7 @@ def test_square_band_shrinks_with_weight(clbm_lib):
     # the 256x64 channel with a 12-side square at (64, 32): the middle band
     # holds the square's rows and gets fewer rows as their weight grows
     d = desc(clbm_lib, 256, 64, 58, 70, 26, 38)
-    assert list(clbm_lib.band_rows(d, 3, 3.0)) == [24, 16, 24]
+    assert list(clbm_lib.band_rows(d, 3, 3.0)) == [24, 15, 25]
     mids = [clbm_lib.band_rows(d, 3, g)[1] for g in (0.0, 0.5, 1.0, 2.0, 3.0, 4.0, 8.0)]
     assert mids == sorted(mids, reverse=True) and mids[-1] < mids[0]
     for g in (0.5, 2.0, 8.0):
