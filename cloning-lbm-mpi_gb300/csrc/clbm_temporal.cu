@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
     }
   }
   __syncthreads();
-  const int range[5] = {count_s[0], count_s[1], count_s[2], count_s[3], count_s[4]};
+  const int *range = count_s;  // read at each loop start: five registers fewer held across the steps
   const float *map = FIELD ? a.maps + R.map_base + (long long)b.clone * R.nodes + (long long)b.row0 * b.W : nullptr;
   bool bad = false;
   cluster.sync();
