@@ -17,8 +17,9 @@ value      device time (CUDA events on the sampler's stream) of K intervals,
            needed between intervals.
 e2e        the same metric through the C ABI as a driver calls it: the initial
            populations loaded from pinned host memory in the reference's AoS
-           FP64 layout, then per interval the drag series, labels, weights and
-           R_t read back to the host.
+           FP64 layout, then every interval's drag series, labels, weights and
+           R_t delivered to host arrays (clbm_run_sampler_outputs: each
+           interval's outputs are copied out while the next interval runs).
 roofline   the dominant kernel (the stream-collide step, or the cluster-resident
            interval kernel when the autotuner picks it): algorithmic bytes
            (72 B/LUP FP32, 144 B/LUP FP64: one read and one write of nine
@@ -518,7 +519,7 @@ def main():
         stream_ref = {"kernel": "k_step_f32", "ms_per_step": sms, "achieved": sa, "frac": sa / peak,
                       "traffic": ncu_traffic(f"k_step_f32_{args.workload}.md")}
 
-    # ---- e2e: initial load from pinned host memory + per-interval host reads ----
+    # ---- e2e: initial load from pinned host memory + every interval's outputs on the host ----
     e2e = None
     if not args.no_e2e:
         n = [9 * r.nodes for r in wl.runs]
@@ -531,7 +532,15 @@ def main():
             one.copy_(torch.from_numpy(s.dump(i, 0)))
             h = one.repeat(r.nclones).pin_memory()
             host.append(h)
-        d2h = 0
+        # every interval's outputs as the reference writes them per interval
+        # (drag series -> data_force.datout, labels, weights; R_t), into host
+        # arrays allocated and touched before the timed region
+        nct = sum(r.nclones for r in wl.runs)
+        out = {"rvalues": np.full((len(wl.runs), args.steps), -1.0),
+               "drag": np.full((args.steps, nct, wl.steps), -1.0),
+               "labels": np.full((args.steps, nct), -1, np.int32),
+               "weights": np.full((args.steps, nct), -1.0)}
+        d2h = sum(a.nbytes for a in out.values())
         torch.cuda.synchronize()
         barrier(world)
         t0 = time.perf_counter()
@@ -539,22 +548,18 @@ def main():
             clbm.check(clbm.lib().clbm_load_run_aos_f64(s.h, i, host[i].data_ptr()), "load")
         load_s = time.perf_counter() - t0
         h2d = sum(h.numel() * 8 for h in host)
-        for _ in range(args.steps):
-            # one interval and its cloning step (a CUDA graph unless --eager)
-            s.run_sampler(wl.steps, 1)
-            for i in range(len(wl.runs)):
-                d = s.drag(i)
-                d2h += d.nbytes
-            for i in range(len(wl.runs)):
-                cr = s.clone_result(i)
-                d2h += cr["labels"].nbytes + cr["weights"].nbytes + 8 + cr["copies_pre"].nbytes * 2
+        # the intervals (CUDA graphs unless --eager), each interval's outputs
+        # copied to the host while the next one runs
+        s.run_sampler_outputs(wl.steps, args.steps, out)
         torch.cuda.synchronize()
         wall = allmax(world, time.perf_counter() - t0)
+        assert (out["labels"] >= 0).all() and np.isfinite(out["drag"]).all()
         e2e = {"value": world * lups_interval * args.steps / wall, "unit": "clone-LUPS/s",
                "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
                "initial_load": {"ms": 1e3 * load_s, "gb_per_s": h2d / load_s / 1e9},
                "note": "initial AoS FP64 populations from pinned host memory (amortised over the "
-                       "steps) + per-interval drag series, labels, weights, copy numbers, R_t"}
+                       "steps) + every interval's drag series, labels, weights and R_t delivered to "
+                       "host arrays (clbm_run_sampler_outputs: staged while the next interval runs)"}
 
     s.close()
     fp64 = None

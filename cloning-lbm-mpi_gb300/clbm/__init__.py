@@ -33,7 +33,7 @@ EXPORTS = [
     "clbm_load_run_aos_f64", "clbm_dump_pops_aos_f64", "clbm_set_snapshots_aos_f64",
     "clbm_init_equilibrium", "clbm_run_interval", "clbm_get_drag", "clbm_clone_step",
     "clbm_get_clone_result", "clbm_get_rvalues", "clbm_intervals_done", "clbm_scgf",
-    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_profile", "clbm_profile_read", "clbm_profile_read_fields", "clbm_autotune", "clbm_set_step_variant", "clbm_set_run_variants", "clbm_get_run_variants", "clbm_band_rows", "clbm_set_band_rows", "clbm_get_band_rows", "clbm_shard_plan", "clbm_ref_random_field",
+    "clbm_set_pending_labels", "clbm_macro_fields", "clbm_get_field_map", "clbm_enable_history", "clbm_reconstruct_lineages", "clbm_drag_fwd", "clbm_drag_bwd", "clbm_get_drag_grad_aos_f64", "clbm_run_sampler", "clbm_run_sampler_outputs", "clbm_profile", "clbm_profile_read", "clbm_profile_read_fields", "clbm_autotune", "clbm_set_step_variant", "clbm_set_run_variants", "clbm_get_run_variants", "clbm_band_rows", "clbm_set_band_rows", "clbm_get_band_rows", "clbm_shard_plan", "clbm_ref_random_field",
     "clbm_error_word", "clbm_sync", "clbm_stream",
 ]
 
@@ -95,6 +95,7 @@ def lib() -> C.CDLL:
         L.clbm_clone_step.argtypes = [vp]
         L.clbm_get_clone_result.argtypes = [vp, i, vp, vp, vp, vp, vp]
         L.clbm_run_sampler.argtypes = [vp, i, i, vp]
+        L.clbm_run_sampler_outputs.argtypes = [vp, i, i, vp, vp, vp, vp]
         L.clbm_get_rvalues.argtypes = [vp, i, i, i, vp, vp]
         L.clbm_intervals_done.argtypes = [vp, i, C.POINTER(i)]
         L.clbm_scgf.argtypes = [vp, i, i, i, d, C.POINTER(d)]
@@ -384,6 +385,21 @@ class Sampler:
         check(lib().clbm_run_sampler(self.h, steps, intervals, _p(rv)), "clbm_run_sampler")
         self.last_steps = steps
         return rv
+
+    def run_sampler_outputs(self, steps: int, intervals: int, out: dict | None = None) -> dict:
+        """clbm_run_sampler_outputs: R_t, and every interval's drag series
+        [interval][clone][step], labels and weights [interval][clone] (all
+        runs' clones in run order).  `out` may hold preallocated arrays."""
+        n = sum(r.nclones for r in self.runs)
+        out = out if out is not None else {}
+        rv = out.setdefault("rvalues", np.empty((len(self.runs), intervals)))
+        drag = out.setdefault("drag", np.empty((intervals, n, steps)))
+        labels = out.setdefault("labels", np.empty((intervals, n), np.int32))
+        weights = out.setdefault("weights", np.empty((intervals, n)))
+        check(lib().clbm_run_sampler_outputs(self.h, steps, intervals, _p(rv), _p(drag), _p(labels), _p(weights)),
+              "clbm_run_sampler_outputs")
+        self.last_steps = steps
+        return out
 
     def autotune(self, launches: int = 5, measure: bool = True):
         """Returns (best variant, ms per launch of every variant)."""

@@ -86,6 +86,11 @@ struct clbm_ctx {
   std::vector<cudaStream_t> side;   // side stream i carries the i-th cluster-resident run
   std::vector<cudaEvent_t> fork_join;  // [0] fork, [1 + i] side stream i done
   bool pending = false;  // a clone step's copies/perturbations await the next interval
+  // pinned staging of clbm_run_sampler_outputs: two slots, each the drag
+  // series (total_clones x max_steps), labels and weights of one interval
+  double *h_drag[2] = {nullptr, nullptr}, *h_weights[2] = {nullptr, nullptr};
+  int *h_labels[2] = {nullptr, nullptr};
+  cudaEvent_t h_ready[2] = {nullptr, nullptr};
   // random body-force fields (forcing variant)
   bool any_field = false;
   float *d_spec = nullptr, *d_maps = nullptr;
@@ -182,6 +187,12 @@ extern "C" int clbm_destroy(clbm_ctx *c) {
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
   for (cudaEvent_t e : c->fev) cudaEventDestroy(e);
+  for (int k = 0; k < 2; k++) {
+    void *hb[] = {c->h_drag[k], c->h_weights[k], c->h_labels[k]};
+    for (void *b : hb)
+      if (b) cudaFreeHost(b);
+    if (c->h_ready[k]) cudaEventDestroy(c->h_ready[k]);
+  }
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return CLBM_OK;
@@ -951,36 +962,93 @@ static int graph_for(clbm_ctx *c, int steps, int sbuf, cudaGraphExec_t *exec) {
   return CLBM_OK;
 }
 
+static int enqueue_sampler_interval(clbm_ctx *c, int steps);
+static int copy_rvalues(clbm_ctx *c, int intervals, double *rvalues);
+
 extern "C" int clbm_run_sampler(clbm_ctx *c, int steps, int intervals, double *rvalues) {
   if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
   if (steps < 1 || steps > c->max_steps || intervals < 0) return fail(CLBM_ERR_INVALID, "bad steps/intervals");
   if (int st = check_snapshots(c)) return st;
-  for (int i = 0; i < intervals; i++) {
-    if ((c->flags & CLBM_FLAG_GRAPH) && !c->profiling) {
-      cudaGraphExec_t ge = nullptr;
-      if (int st = graph_for(c, steps, c->s_buf, &ge)) return st;
-      CK(cudaGraphLaunch(ge, c->stream));
-    } else {
-      CK(enqueue_interval(c, steps, c->s_buf, c->profiling));
-      CK(enqueue_clone(c));
-    }
-    c->s_buf = sbuf_after(c->s_buf, steps);
-    c->last_steps = steps;
-    c->pending = true;
-  }
+  for (int i = 0; i < intervals; i++)
+    if (int st = enqueue_sampler_interval(c, steps)) return st;
   if (int st = check_error_word(c)) return st;
-  if (rvalues && intervals > 0) {
-    for (int r = 0; r < c->nruns; r++) {
-      int f = 0;
-      CK(cudaMemcpyAsync(&f, &c->d.state[r].interval, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-      CK(cudaStreamSynchronize(c->stream));
-      f -= intervals;
-      if (f < 0 || f + intervals > c->d.max_intervals) return fail(CLBM_ERR_INVALID, "R_t history capacity exceeded");
-      CK(cudaMemcpyAsync(rvalues + (size_t)r * intervals, c->d.rvalues + (size_t)r * c->d.max_intervals + f,
-                         sizeof(double) * intervals, cudaMemcpyDeviceToHost, c->stream));
-    }
-    CK(cudaStreamSynchronize(c->stream));
+  if (rvalues && intervals > 0) return copy_rvalues(c, intervals, rvalues);
+  return CLBM_OK;
+}
+
+// One interval (and its cloning step) on the context's stream: a CUDA graph
+// under CLBM_FLAG_GRAPH (eager while profiling), else launch by launch.
+static int enqueue_sampler_interval(clbm_ctx *c, int steps) {
+  if ((c->flags & CLBM_FLAG_GRAPH) && !c->profiling) {
+    cudaGraphExec_t ge = nullptr;
+    if (int st = graph_for(c, steps, c->s_buf, &ge)) return st;
+    CK(cudaGraphLaunch(ge, c->stream));
+  } else {
+    CK(enqueue_interval(c, steps, c->s_buf, c->profiling));
+    CK(enqueue_clone(c));
   }
+  c->s_buf = sbuf_after(c->s_buf, steps);
+  c->last_steps = steps;
+  c->pending = true;
+  return CLBM_OK;
+}
+
+// R_t of the last `intervals` intervals of every run ([run][interval]).
+static int copy_rvalues(clbm_ctx *c, int intervals, double *rvalues) {
+  for (int r = 0; r < c->nruns; r++) {
+    int f = 0;
+    CK(cudaMemcpyAsync(&f, &c->d.state[r].interval, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    f -= intervals;
+    if (f < 0 || f + intervals > c->d.max_intervals) return fail(CLBM_ERR_INVALID, "R_t history capacity exceeded");
+    CK(cudaMemcpyAsync(rvalues + (size_t)r * intervals, c->d.rvalues + (size_t)r * c->d.max_intervals + f,
+                       sizeof(double) * intervals, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return CLBM_OK;
+}
+
+extern "C" int clbm_run_sampler_outputs(clbm_ctx *c, int steps, int intervals, double *rvalues, double *drag,
+                                        int *labels, double *weights) {
+  if (!c) return fail(CLBM_ERR_INVALID, "ctx is NULL");
+  if (steps < 1 || steps > c->max_steps || intervals < 0) return fail(CLBM_ERR_INVALID, "bad steps/intervals");
+  if (int st = check_snapshots(c)) return st;
+  const size_t nc = (size_t)c->total_clones;
+  for (int k = 0; k < 2; k++) {
+    if (!c->h_drag[k]) CK(cudaHostAlloc((void **)&c->h_drag[k], sizeof(double) * nc * c->max_steps, cudaHostAllocDefault));
+    if (!c->h_weights[k]) CK(cudaHostAlloc((void **)&c->h_weights[k], sizeof(double) * nc, cudaHostAllocDefault));
+    if (!c->h_labels[k]) CK(cudaHostAlloc((void **)&c->h_labels[k], sizeof(int) * nc, cudaHostAllocDefault));
+    if (!c->h_ready[k]) CK(cudaEventCreateWithFlags(&c->h_ready[k], cudaEventDisableTiming));
+  }
+  // interval i's outputs: device -> staging slot i % 2 right after the
+  // interval (stream order: before interval i + 1 overwrites them), then,
+  // once interval i + 1 is enqueued, staging -> the caller's arrays on the
+  // host while the device runs it
+  auto deliver = [&](int i) -> int {
+    const int k = i & 1;
+    CK(cudaEventSynchronize(c->h_ready[k]));
+    if (drag) std::memcpy(drag + (size_t)i * nc * steps, c->h_drag[k], sizeof(double) * nc * steps);
+    if (labels) std::memcpy(labels + (size_t)i * nc, c->h_labels[k], sizeof(int) * nc);
+    if (weights) std::memcpy(weights + (size_t)i * nc, c->h_weights[k], sizeof(double) * nc);
+    return CLBM_OK;
+  };
+  for (int i = 0; i < intervals; i++) {
+    if (int st = enqueue_sampler_interval(c, steps)) return st;
+    const int k = i & 1;
+    cudaStream_t s = c->stream;
+    if (drag)
+      CK(cudaMemcpy2DAsync(c->h_drag[k], sizeof(double) * steps, c->d.drag, sizeof(double) * c->max_steps,
+                           sizeof(double) * steps, nc, cudaMemcpyDeviceToHost, s));
+    if (labels) CK(cudaMemcpyAsync(c->h_labels[k], c->d.labels, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
+    if (weights) CK(cudaMemcpyAsync(c->h_weights[k], c->d.weights, sizeof(double) * nc, cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(c->h_ready[k], s));
+    if (i > 0)
+      if (int st = deliver(i - 1)) return st;
+  }
+  if (intervals > 0)
+    if (int st = deliver(intervals - 1)) return st;
+  if (int st = check_error_word(c)) return st;
+  if (rvalues && intervals > 0) return copy_rvalues(c, intervals, rvalues);
   return CLBM_OK;
 }
 

@@ -261,6 +261,20 @@ int clbm_intervals_done(clbm_ctx *ctx, int run, int *done);
  * CUDA graphs when the context was created with CLBM_FLAG_GRAPH.  rvalues
  * (nullable, [nruns][intervals]) receives R_t of every interval. */
 int clbm_run_sampler(clbm_ctx *ctx, int steps, int intervals, double *rvalues);
+/* clbm_run_sampler that also delivers every interval's outputs to host
+ * arrays without stalling the device: after each interval and its cloning
+ * step the outputs are copied to pinned staging memory on the context's
+ * stream, and from there into the caller's arrays on the host while the
+ * device runs the next interval (the reference writes them per interval:
+ * data_force.datout from the drag series, labels.dat, the weights;
+ * src/mpi_LBM_GK_pops_perturb.cpp:445-520).  With T = steps and N = the
+ * total clones of all runs, interval i writes (any pointer nullable):
+ * drag + i*N*T the drag series, run after run and clone after clone, T
+ * values each (clbm_get_drag's layout); labels + i*N the cloning step's
+ * parent labels and weights + i*N the weights (clbm_get_clone_result's);
+ * rvalues as clbm_run_sampler.  The caller's arrays may be pageable. */
+int clbm_run_sampler_outputs(clbm_ctx *ctx, int steps, int intervals, double *rvalues,
+                             double *drag, int *labels, double *weights);
 
 /* Timing of the interval kernels: while enabled, every interval enqueued
  * eagerly (run_interval, or run_sampler without CUDA graphs) records a CUDA

@@ -159,6 +159,40 @@ def test_graph_replay_equals_eager(gpu, clbm_lib, orc, prec):
     assert np.array_equal(out[0][2], out[1][2])
 
 
+@pytest.mark.parametrize("prec,flags", [(0, 0), (1, 1)])
+def test_run_sampler_outputs_equals_per_interval_reads(gpu, clbm_lib, orc, prec, flags):
+    """clbm_run_sampler_outputs (outputs staged while the next interval runs)
+    delivers exactly what per-interval clbm_run_sampler + clbm_get_drag +
+    clbm_get_clone_result read, on an uneven two-run batch."""
+    cases = [channel_case(orc, W=48, H=16, side=4, nc=4, k=3.0, T=30, n=5, seed=21),
+             channel_case(orc, W=72, H=24, side=6, nc=6, k=-2.0, T=30, n=5, seed=22)]
+    descs = [desc(clbm_lib, g, nc, perturb_mode=2, eps=1e-4, seed=seed, **phys)
+             for (g, phys, T, n, nc, seed) in cases]
+    T, n = 30, 5
+    ref = {"drag": [], "labels": [], "weights": [], "rv": []}
+    with clbm_lib.Sampler(descs, prec, max_steps=T, flags=flags) as s:
+        for r, c in enumerate(cases):
+            s.init_equilibrium(r, 0.05, 1e-3, c[5])
+        for t in range(n):
+            ref["rv"].append(s.run_sampler(T, 1)[:, 0])
+            ref["drag"].append(np.concatenate([s.drag(r) for r in range(2)]))
+            crs = [s.clone_result(r) for r in range(2)]
+            ref["labels"].append(np.concatenate([c["labels"] for c in crs]))
+            ref["weights"].append(np.concatenate([c["weights"] for c in crs]))
+        ref_state = s.dump(1, 2)
+    with clbm_lib.Sampler(descs, prec, max_steps=T, flags=flags) as s:
+        for r, c in enumerate(cases):
+            s.init_equilibrium(r, 0.05, 1e-3, c[5])
+        first = s.run_sampler_outputs(T, 2)
+        rest = s.run_sampler_outputs(T, n - 2)
+        assert s.error_word() == 0
+        assert np.array_equal(s.dump(1, 2), ref_state)
+    for key, k2 in (("drag", "drag"), ("labels", "labels"), ("weights", "weights")):
+        got = np.concatenate([first[k2], rest[k2]])
+        assert np.array_equal(got, np.stack(ref[key])), key
+    assert np.array_equal(np.concatenate([first["rvalues"], rest["rvalues"]], axis=1), np.stack(ref["rv"], axis=1))
+
+
 def test_fp32_against_fp64_oracle(gpu, clbm_lib, orc):
     """FP32 populations (stored as f - w) with FP64 drag integral: first
     interval drag series within 1e-5 relative of the FP64 oracle."""
