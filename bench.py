@@ -507,8 +507,12 @@ def main():
     # DRAM bytes per launch of the dominant kernel (one step for the streaming
     # kernel, one interval of wl.steps steps for the cluster-resident one)
     traffic = ncu_traffic(f"{vinfo['kernel']}_{args.workload}.md")
-    # reseed + the interval kernels + drag reduction (2) + cloning step
-    launches_per_interval = n_cluster + (wl.steps if any_stream else 0) + 4
+    # the interval kernels + drag reduction (2) + cloning step, + the reseed
+    # unless every run is cluster-resident with an even interval length (the
+    # interval kernels then do the reseed while loading their clones)
+    fused = (wl.precision == clbm.FP32 and not any_stream and wl.steps % 2 == 0
+             and not any(r.field_steps > 0 for r in wl.runs))
+    launches_per_interval = n_cluster + (wl.steps if any_stream else 0) + (3 if fused else 4)
     # the streaming step kernel's own roofline, from the autotuner's timing of
     # its best launch variant on this workload (one launch per step)
     stream_ref = None

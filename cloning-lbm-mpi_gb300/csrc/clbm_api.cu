@@ -685,8 +685,11 @@ static cudaError_t ensure_side(clbm_ctx *c, int n) {
 // S_T left in buffer dst; the streaming runs alternate between the two
 // buffers as the pull scheme does and store S on their last step.  timing
 // (autotuner): every streaming launch reads src and writes the other buffer
-// and none is a last step, so the state in src is left untouched.
-static cudaError_t enqueue_lb_steps(clbm_ctx *c, const LbPlan &p, int steps, int src, int dst, bool timing) {
+// and none is a last step, so the state in src is left untouched.  fuse
+// (cluster-resident runs only): the kernels form P_0 themselves from the
+// reseed's inputs (fuse->src, a buffer other than dst) instead of reading src.
+static cudaError_t enqueue_lb_steps(clbm_ctx *c, const LbPlan &p, int steps, int src, int dst, bool timing,
+                                    const ReseedArgs *fuse = nullptr) {
   const bool f64 = c->precision == CLBM_FP64;
   cudaStream_t s = c->stream;
   cudaError_t e;
@@ -703,7 +706,7 @@ static cudaError_t enqueue_lb_steps(clbm_ctx *c, const LbPlan &p, int steps, int
     cudaStream_t ts = c->side[i];
     if ((e = cudaStreamWaitEvent(ts, c->fork_join[0], 0)) != cudaSuccess) return e;
     TemporalArgs ta{R, r, steps, (const float *)c->pop[src], (float *)c->pop[dst], (float *)c->d.terms,
-                    c->d.term_slab, c->d.err, c->d_maps, {}};
+                    c->d.term_slab, c->d.err, c->d_maps, {}, fuse ? 1 : 0, fuse ? *fuse : ReseedArgs{}};
     const int cs = p.cs[r];
     if (r < (int)p.rows.size() && (int)p.rows[r].size() == cs + 1)
       std::copy(p.rows[r].begin(), p.rows[r].end(), ta.band_row0);
@@ -783,7 +786,15 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
   }
   ReseedArgs ra{c->d.runs, c->nruns, S, c->pop[1 - sbuf], c->d.labels, c->d.mark, c->d.pert,
                 c->d.prefactors, c->d.snaps, c->d.state, c->d.err, c->d_maps};
-  if ((e = launch_reseed(f64, ra, c->total_blocks, s)) != cudaSuccess) return e;
+  const LbPlan plan = current_plan(c, f64);
+  // Every run cluster-resident under the uniform body force and an even step
+  // count (S_T then goes to the other buffer than S): the interval kernels do
+  // the reseed while loading their clones, which saves writing P_0 and
+  // reading it back.  (With an odd count S_T would overwrite S while other
+  // clusters still copy parents.)
+  bool fuse = !f64 && !c->any_field && steps % 2 == 0;
+  for (int r = 0; r < c->nruns; r++) fuse = fuse && plan.cs[r] > 0;
+  if (!fuse && (e = launch_reseed(f64, ra, c->total_blocks, s)) != cudaSuccess) return e;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (prof) {
     if ((size_t)c->ev_used + 2 > c->ev.size()) {
@@ -804,8 +815,8 @@ static cudaError_t enqueue_interval(clbm_ctx *c, int steps, int sbuf, bool prof 
   // one launch each on its own side stream; the streaming runs meanwhile one
   // step launch per step on the main stream; the side streams join before the
   // drag reduction (a captured interval holds them as parallel branches).
-  const LbPlan plan = current_plan(c, f64);
-  if ((e = enqueue_lb_steps(c, plan, steps, 1 - sbuf, (steps % 2 == 1) ? sbuf : 1 - sbuf, false)) != cudaSuccess)
+  if ((e = enqueue_lb_steps(c, plan, steps, 1 - sbuf, (steps % 2 == 1) ? sbuf : 1 - sbuf, false,
+                            fuse ? &ra : nullptr)) != cudaSuccess)
     return e;
   if (prof && (e = cudaEventRecord(e1, s)) != cudaSuccess) return e;
   if ((e = launch_drag_reduce(f64, c->d, c->nruns, c->total_clones, steps, c->any_stress, c->any_momentum, s)) != cudaSuccess) return e;

@@ -80,6 +80,21 @@ struct StepArgs {
   const float *maps;  // random body-force fields (nullable)
 };
 
+struct ReseedArgs {
+  const RunDev *runs;
+  int nruns;
+  const void *src;    // pre-collision state S of every slot's parent
+  void *dst;          // post-collision populations P of the next interval's first step
+  const int *labels;
+  const int *mark;
+  const double *pert;       // (weight, 1/a) per clone
+  const double *prefactors; // [clone][MAX_SNAP]
+  const double *snaps;
+  const RunState *state;    // interval counter
+  unsigned *err;
+  const float *maps;        // random body-force fields (nullable)
+};
+
 // largest cluster of the cluster-resident interval kernel (non-portable size)
 constexpr int MAX_CLUSTER = 16;
 
@@ -96,22 +111,13 @@ struct TemporalArgs {
   // band b of a clone (CTA of cluster rank b) holds the lattice rows
   // [band_row0[b], band_row0[b + 1]); band_row0[cs] = H
   int band_row0[MAX_CLUSTER + 1];
+  // fused: the kernel forms P_0 itself from the previous interval's S in
+  // rs.src (parent copy, perturbation, first collision: the reseed of every
+  // node, clbm_step.cu), instead of reading it from src
+  int fused;
+  ReseedArgs rs;
 };
 
-struct ReseedArgs {
-  const RunDev *runs;
-  int nruns;
-  const void *src;    // pre-collision state S of every slot's parent
-  void *dst;          // post-collision populations P of the next interval's first step
-  const int *labels;
-  const int *mark;
-  const double *pert;       // (weight, 1/a) per clone
-  const double *prefactors; // [clone][MAX_SNAP]
-  const double *snaps;
-  const RunState *state;    // interval counter
-  unsigned *err;
-  const float *maps;        // random body-force fields (nullable)
-};
 
 // kernel launchers (clbm_step.cu, clbm_cloning.cu)
 cudaError_t launch_step(bool f64, bool last, const StepArgs &a, int blocks, cudaStream_t s,

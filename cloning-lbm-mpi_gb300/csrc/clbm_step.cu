@@ -17,6 +17,7 @@
 
 #include "clbm_internal.h"
 #include "clbm_physics.cuh"
+#include "clbm_reseed.cuh"
 
 namespace clbm {
 
@@ -44,34 +45,6 @@ __device__ __forceinline__ NodeLoc locate(const RunDev *runs, int nruns) {
   L.y = (int)__umulhi((unsigned)L.n, R.div_w);
   L.x = L.n - L.y * R.W;
   return L;
-}
-
-template <bool F64>
-using pop_t = typename std::conditional<F64, double, float>::type;
-
-// map: the node's random-field value when the collision is under the
-// spatial force, beta(x,y) = (1 + eps*map)*beta0 (streamCollCompute.cpp:63)
-template <bool F64>
-__device__ __forceinline__ void collide_node(const RunDev &R, const pop_t<F64> S[9],
-                                             pop_t<F64> P[9], const float *map = nullptr) {
-  if constexpr (F64) {
-    if (map) {
-      const double beta = DMUL(DADD(1.0, DMUL(R.field_eps, (double)*map)), R.beta);
-      double wcb[9];
-#pragma unroll
-      for (int k = 0; k < 9; k++) wcb[k] = DMUL(DMUL(w_of(k), R.cforce), beta);
-      collide_ref64(S, P, beta, wcb, R.omega, R.om1);
-    } else {
-      collide_ref64(S, P, R.beta, R.wcb, R.omega, R.om1);
-    }
-  } else {
-    collide_f32_run(R, S, P, map, R.f_field_eps);
-  }
-}
-
-__device__ __forceinline__ const float *node_map(const float *maps, const RunDev &R, int clone, int n,
-                                                 bool on) {
-  return (on && maps) ? maps + R.map_base + (long long)clone * R.nodes + n : nullptr;
 }
 
 template <bool F64>
@@ -272,10 +245,6 @@ cudaError_t launch_step(bool f64, bool last, const StepArgs &a, int blocks, cuda
 // S(labels[j]) (the clone copy, pops driver :658-701), new clones are
 // perturbed (:412-416: snapshot mix, generatePerturbedState.cpp:4-38, or the
 // counter-based uniform noise), and the result is collided into P.
-__device__ __forceinline__ uint32_t aos_index(const RunDev &R, int x, int y, int k) {
-  return (uint32_t)(k + 9 * (y + R.H * x));
-}
-
 template <bool F64>
 __global__ void __launch_bounds__(STEP_BLOCK) k_reseed(ReseedArgs a) {
   using T = pop_t<F64>;
@@ -285,43 +254,11 @@ __global__ void __launch_bounds__(STEP_BLOCK) k_reseed(ReseedArgs a) {
   const int x = L.x, y = L.y, n = L.n;
   const bool solid = x > R.xmin && x < R.xmax && y > R.ymin && y < R.ymax;
   if (solid) return;  // post-collision values of interior nodes are never pulled
-  const int gclone = R.clone_base + L.clone;
-  int parent = a.labels[gclone];
-  if (parent < 0 || parent >= R.nclones) {
-    atomicOr(a.err, (unsigned)ERR_BAD_PARENT);
-    parent = L.clone;
-  }
-  const long long plane = R.plane;
-  const T *src = (const T *)a.src + R.pop_base + (long long)parent * 9 * plane;
-  T *dst = (T *)a.dst + R.pop_base + (long long)L.clone * 9 * plane;
-  T S[9];
-#pragma unroll
-  for (int k = 0; k < 9; k++) S[k] = src[k * plane + n];
-  if (R.perturb_mode != 0 && a.mark[gclone]) {
-    const int interval = a.state[L.run].interval;
-    const double *pre = a.prefactors + (long long)gclone * MAX_SNAP;
-    const double wgt = a.pert[2 * gclone], inv_a = a.pert[2 * gclone + 1];
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      double f = F64 ? (double)S[k] : w_of(k) + (double)S[k];
-      if (R.perturb_mode == 2) {
-        const double u = philox_uniform(R.seed, aos_index(R, x, y, k), (uint32_t)L.clone,
-                                        (uint32_t)interval, (R.run_id << 4) | DOM_PERTURB);
-        f = DMUL(f, DADD(1.0, DMUL(R.eps, DSUB(DMUL(2.0, u), 1.0))));
-      } else {
-        // S = sum_q r_q snap_q in snapshot order; f <- (f + eps*S*weight) / a
-        const double *sp = a.snaps + R.snap_base + (long long)k * plane + n;
-        double mix = DMUL(pre[0], sp[0]);
-        for (int q = 1; q < R.nsnap; q++) mix = DADD(mix, DMUL(pre[q], sp[(long long)q * 9 * plane]));
-        f = DMUL(DADD(f, DMUL(DMUL(R.eps, mix), wgt)), inv_a);
-      }
-      S[k] = F64 ? (T)f : (T)(f - w_of(k));
-    }
-  }
   T P[9];
-  collide_node<F64>(R, S, P, node_map(a.maps, R, L.clone, n, R.field_mode && R.field_steps > 0));
+  reseed_node<F64>(a, R, L.run, L.clone, x, y, n, P);
+  T *dst = (T *)a.dst + R.pop_base + (long long)L.clone * 9 * R.plane;
 #pragma unroll
-  for (int k = 0; k < 9; k++) dst[k * plane + n] = P[k];
+  for (int k = 0; k < 9; k++) dst[k * R.plane + n] = P[k];
 }
 
 cudaError_t launch_reseed(bool f64, const ReseedArgs &a, int blocks, cudaStream_t s) {

@@ -27,6 +27,7 @@
 
 #include "clbm_internal.h"
 #include "clbm_physics.cuh"
+#include "clbm_reseed.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -251,6 +252,27 @@ __device__ __forceinline__ void load_band(const Band &b, float *A) {
   }
 }
 
+// P_0 formed here from the previous interval's S (fused reseed: parent copy,
+// perturbation, first collision; the same per-node function as the reseed
+// kernel, so bit-identical), in the same layout.  Square-interior nodes get
+// zeros: their slots are never read before the last step writes them.
+template <int THREADS>
+__device__ __forceinline__ void load_band_reseed(const TemporalArgs &a, const Band &b, float *A) {
+  const RunDev &R = a.rd;
+  for (int i = threadIdx.x; i < b.nb; i += THREADS) {
+    const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * b.W, y = b.row0 + ly;
+    float P[9];
+    if (x > R.xmin && x < R.xmax && y > R.ymin && y < R.ymax) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) P[k] = 0.0f;
+    } else {
+      reseed_node<false>(a.rs, R, a.run, b.clone, x, y, y * b.W + x, P);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) A[i * 9 + opp_of(k)] = P[k];
+  }
+}
+
 // One node away from the square, not the last step of the interval.  C, U,
 // D = the node's row and the rows above (y-1) and below (y+1); om, o0, op =
 // the column offsets of x-1, x, x+1 (times 9).  GATHER: S(n,k) = A[n -
@@ -471,7 +493,12 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
   cg::cluster_group cluster = cg::this_cluster();
   const Band b = make_band(a, A, cluster);
   const RunDev &R = a.rd;
-  load_band<THREADS>(b, A);
+  // (the fused load is compiled into the uniform-force kernels only: in the
+  // random-field ones it raised register spills in the step loop)
+  if (!FIELD && a.fused)
+    load_band_reseed<THREADS>(a, b, A);
+  else
+    load_band<THREADS>(b, A);
   const int nseg = (b.nb + 31) / 32;
   unsigned short *list = (unsigned short *)(A + (size_t)9 * b.nb);
   unsigned char *cls = (unsigned char *)(list + ((nseg + 7) & ~7));

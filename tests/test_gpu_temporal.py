@@ -200,3 +200,50 @@ def test_band_rows_checks(gpu, clbm_lib, orc):
         s.set_band_rows(0, [5, 19])
         s.set_step_variant(temporal_variant(2, 0))  # a variant change restores the even split
         assert list(s.band_rows(0)) == [12, 12]
+
+
+@pytest.mark.parametrize("W,H,side,xc,yc,cs,tv,mode,field,T,flags", [
+    (64, 24, 6, 16, 12, 2, 0, "uniform", False, 20, 0),
+    (96, 23, 5, 30, 9, 3, 1, "mix", False, 22, 1),
+    (64, 24, 6, 16, 12, 4, 2, "uniform", True, 20, 1),
+    (200, 50, 8, 50, 25, 8, 1, "none", False, 10, 0),
+])
+def test_fused_reseed_equals_streaming(gpu, clbm_lib, orc, W, H, side, xc, yc, cs, tv, mode, field, T, flags):
+    """Every run cluster-resident and an even interval length: the interval
+    kernel forms P_0 itself (parent copy, perturbation -- counter-based or
+    snapshot mix --, first collision) while loading its clone, with no reseed
+    launch (a random-field run keeps the reseed kernel); bit-identical to the
+    streaming path, which runs the reseed kernel, over three intervals with
+    cloning steps."""
+    g = orc.channel_geom(W, H, side, xc, yc)
+    u0, nc = 0.05, 6
+    pm = {"uniform": clbm_lib.PERTURB_UNIFORM, "mix": clbm_lib.PERTURB_MIX, "none": clbm_lib.PERTURB_NONE}[mode]
+    d = clbm_lib.RunDesc(width=g.nx, height=g.ny, xmin=g.xmin, xmax=g.xmax, ymin=g.ymin, ymax=g.ymax,
+                         nclones=nc, ranks=1, tau=0.57, beta=side * u0 * u0 / ((W - 1) * (H - 1)), alpha=12.0,
+                         force_scale=2 / (u0 * u0 * side), dt=u0 / side, perturb_mode=pm,
+                         eps=1e-3 if mode == "uniform" else 0.01, seed=3, nsnap=4 if mode == "mix" else 0)
+    if field:
+        d.field_mode, d.field_steps, d.field_eps, d.field_sigma = 1, 7, 0.2, 6.0
+    snaps = np.concatenate([orc.init_equilibrium(g, u0, 2e-2, 5, 0, j) for j in range(4)]) if mode == "mix" else None
+    out = []
+    for variant in (4, temporal_variant(cs, tv)):
+        with clbm_lib.Sampler([d], clbm_lib.FP32, max_steps=T, flags=flags) as s:
+            s.set_step_variant(variant)
+            s.init_equilibrium(0, u0, 1e-3, 7)
+            if snaps is not None:
+                s.set_snapshots(0, snaps)
+            res = []
+            for t in range(3):
+                s.run_interval(T)
+                res.append(s.drag(0))
+                s.clone_step()
+                cr = s.clone_result(0)
+                res.append(cr["labels"].astype(np.float64))
+                res.append(cr["weights"])
+            res.extend(s.dump(0, j) for j in range(nc))
+            assert s.error_word() == 0
+            out.append(res)
+    # some slot took another's state (the copy is exercised)
+    assert any(not np.array_equal(out[0][i], np.arange(nc)) for i in (1, 4, 7))
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
