@@ -474,15 +474,16 @@ __device__ __forceinline__ void band_step(const TemporalArgs &a, const Band &b, 
 }
 
 // Generic kernel: any W.  The band's nodes form 32-node segments; segments
-// that need update_general (walls, band edges, the square's box) cost several
-// times a bulk segment, so they are dealt out first, one per warp, and the
-// bulk segments fill in after them: entry k of the list goes to warp k % NW.
-// The step time is that of the slowest warp (every step ends at a cluster
+// that cost more than a bulk segment (the square's box on the general path,
+// then walls and band edges) are dealt out first, one per warp, and the bulk
+// segments fill in after them: entry k of the list goes to warp k % NW.  The
+// step time is that of the slowest warp (every step ends at a cluster
 // barrier), which this keeps near the mean.  (Measured on a 256x64 channel,
-// all slower than this: fast paths for band-edge and wall rows through
-// distributed shared memory, a cost-weighted water-filling of the bulk
-// segments over the warps, a fixed column per thread with compile-time
-// shared-memory offsets.)
+// all slower than this: band-edge and wall rows through generic
+// distributed-shared-memory pointers, a cost-weighted water-filling of the
+// bulk segments over the warps, a fixed column per thread with compile-time
+// shared-memory offsets, segments taken from a shared counter in one
+// dispatch loop, the band geometry in shared memory.)
 template <int THREADS, int MINB, bool FIELD>
 __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) {
   // A[node * 9 + k]: a node's nine values together (stride 9 words: no bank
