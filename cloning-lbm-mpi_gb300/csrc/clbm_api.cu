@@ -1377,6 +1377,8 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
       if (e == cudaSuccess) e = time_plan(c, p, tsteps, e0, e1, &run_best);
       if (e != cudaSuccess) return bail(e);
       p.nstream = 0;
+      int ccs = 0, ctv = 0;  // the run's fastest cluster shape, even if streaming beats it
+      double cbest = 1e30;
       for (const int cs : kClusterSizes)
         for (int tv = 0; tv < ntv; tv++) {
           if (!shape_fits(c->runs_h[r], cs, tv)) continue;
@@ -1387,18 +1389,23 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
             cudaGetLastError();
             continue;
           }
+          if (per < cbest) {
+            cbest = per;
+            ccs = cs;
+            ctv = tv;
+          }
           if (per < run_best) {
             run_best = per;
             pcs[r] = cs;
             ptv[r] = tv;
           }
         }
-      if (pcs[r] > 0) {  // the run's own best shape, balanced
-        p.cs[r] = pcs[r];
-        p.tv[r] = ptv[r];
+      if (ccs > 0) {  // that shape balanced: it may beat streaming where the even split does not
+        p.cs[r] = ccs;
+        p.tv[r] = ctv;
         p.rows.assign(R, std::vector<int>());
         for (double g : kBalanceGamma) {
-          std::vector<int> row0 = balanced_split(c->runs_h[r], pcs[r], ptv[r], g);
+          std::vector<int> row0 = balanced_split(c->runs_h[r], ccs, ctv, g);
           if (row0.empty() || row0 == p.rows[r]) continue;
           p.rows[r] = row0;
           double per = 0.0;
@@ -1406,9 +1413,12 @@ extern "C" int clbm_autotune(clbm_ctx *c, int launches, int *best, double *ms_pe
           if (te != cudaSuccess) return bail(te);
           if (per < run_best) {
             run_best = per;
+            pcs[r] = ccs;
+            ptv[r] = ctv;
             prows[r] = row0;
           }
         }
+        if (pcs[r] != ccs || ptv[r] != ctv) prows[r].clear();  // another shape (or streaming) won
       }
       any = any || pcs[r] > 0;
     }
