@@ -215,7 +215,7 @@ def shard_plan(labels: np.ndarray, nshards: int, shard: int) -> dict:
 # thread counts 1024, 512, 256 (one launch per run per interval).
 STREAM_VARIANTS = 8
 TEMPORAL_THREADS = (1024, 512, 256)
-CLUSTER_SIZES = (1, 2, 4, 8, 16, 3, 5, 6, 7)  # the autotuner's numbering order
+CLUSTER_SIZES = (1, 2, 4, 8, 16, 3, 5, 6, 7, 9, 10)  # the autotuner's numbering order
 
 
 def band_rows(run: RunDesc, cluster_size: int, gamma: float) -> np.ndarray:

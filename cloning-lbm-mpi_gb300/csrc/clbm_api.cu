@@ -1123,10 +1123,11 @@ extern "C" int clbm_profile_read_fields(clbm_ctx *c, double *field_ms, int *nint
 // launches; after them, for each cluster size of kClusterSizes in that order,
 // the cluster-resident interval kernel's thread configurations.  The sizes
 // that are not powers of two come last, so the numbers of the others do not
-// move.  A cluster of 4 fills only the GPCs whose SM count is a multiple of
-// 4 (36 resident clusters of 4 = 144 of GB300's 152 SMs); 3, 5, 6 and 7 pack
-// the GPCs differently and change the rows per band.
-static const int kClusterSizes[] = {1, 2, 4, 8, 16, 3, 5, 6, 7};
+// move.  The GPCs' SM counts set how many clusters of a size are resident
+// (one CTA per SM, GB300's 152 SMs): 2 -> 152 SMs busy, 3 -> 138, 4 -> 144,
+// 5 -> 140, 6 -> 138, 7 -> 105, 8 -> 120, 9 -> 135, 10 -> 130, 11 to 16 ->
+// 88 to 112; 9 and 10 serve lattices too large for 8 CTAs' shared memory.
+static const int kClusterSizes[] = {1, 2, 4, 8, 16, 3, 5, 6, 7, 9, 10};
 static constexpr int kNumClusterSizes = (int)(sizeof(kClusterSizes) / sizeof(kClusterSizes[0]));
 
 static int variant_count() { return step_variant_count() + kNumClusterSizes * temporal_variant_count(); }

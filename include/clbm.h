@@ -296,8 +296,8 @@ int clbm_profile_read_fields(clbm_ctx *ctx, double *field_ms, int *nintervals);
  * step), then the cluster-resident interval kernel (every clone's populations
  * in the shared memory of one thread-block cluster for all the steps of an
  * interval, one launch per interval) for cluster sizes 1, 2, 4, 8, 16, 3, 5,
- * 6, 7 (numbered in that order) and three thread counts (1024, 512, 256),
- * where every lattice fits: at most 8 + 27 uniform variants.  For the fastest
+ * 6, 7, 9, 10 (numbered in that order) and three thread counts (1024, 512,
+ * 256), where every lattice fits: at most 8 + 33 uniform variants.  For the fastest
  * cluster-resident shapes it then times band splits balanced for the extra
  * cost of the square's rows and the walls (clbm_band_rows).  With several runs
  * it then times each run alone on every shape that fits its lattice (and its

@@ -85,7 +85,7 @@ def test_autotuned_plan_is_bit_identical(gpu, clbm_lib, orc):
     def tune(s):
         best, ms = s.autotune(launches=3)
         picked["best"] = best
-        assert len(ms) == 8 + 27
+        assert len(ms) == 8 + 33
 
     tuned, variants = run(clbm_lib, orc, tune)
     if picked["best"] != clbm_lib.VARIANT_PER_RUN:
@@ -100,7 +100,7 @@ def test_run_variant_checks(gpu, clbm_lib, orc):
         with pytest.raises(clbm_lib.ClbmError):  # two streaming launch variants
             s.set_run_variants([4, 5, 4, 4, 4])
         with pytest.raises(clbm_lib.ClbmError):  # no such variant
-            s.set_run_variants([4, 4, 4, 8 + 27, 4])
+            s.set_run_variants([4, 4, 4, 8 + 33, 4])
         assert list(s.run_variants()) == [0] * 5
     with clbm_lib.Sampler(d, clbm_lib.FP64, max_steps=10) as s:
         with pytest.raises(clbm_lib.ClbmError):  # cluster-resident intervals are FP32 only

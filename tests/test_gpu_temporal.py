@@ -14,7 +14,7 @@ NSTREAM = 8   # streaming launch variants come first in the autotuner's numberin
 NTHREAD = 3   # thread configurations of the cluster-resident kernel (1024, 512, 256)
 
 
-CLUSTER_SIZES = (1, 2, 4, 8, 16, 3, 5, 6, 7)  # the autotuner's order
+CLUSTER_SIZES = (1, 2, 4, 8, 16, 3, 5, 6, 7, 9, 10)  # the autotuner's order
 
 
 def temporal_variant(cs, tv=0):
@@ -39,6 +39,8 @@ def temporal_variant(cs, tv=0):
     (96, 23, 5, 30, 9, 5, 1, True),
     (200, 50, 8, 50, 25, 6, 2, False),
     (64, 32, 6, 20, 16, 7, 1, False),
+    (200, 50, 8, 50, 25, 9, 0, False),      # non-portable cluster sizes
+    (96, 23, 5, 30, 9, 10, 2, True),
 ])
 def test_temporal_equals_streaming(gpu, clbm_lib, orc, W, H, side, xc, yc, cs, tv, field):
     g = orc.channel_geom(W, H, side, xc, yc)
