@@ -140,10 +140,13 @@ __device__ __forceinline__ void update_general(const TemporalArgs &a, const Band
 // outside the channel or the target inside the square (the push is dropped,
 // as in update_general).  PLAIN: a node off the walls and the square's box
 // (a band-edge row): nothing bounces back and no push is dropped, only the
-// neighbour rows may lie in the adjacent CTAs.
-template <bool PLAIN = false>
+// neighbour rows may lie in the adjacent CTAs.  LOCAL: the node's row and
+// both neighbour rows are in this CTA (1 <= ly <= rows - 2): the same slots
+// through plain shared-memory indexing of A, which the compiler schedules
+// freely (the shared::cluster accesses are ordered asm).
+template <bool PLAIN = false, bool LOCAL = false>
 __device__ __forceinline__ void update_general_gather(const TemporalArgs &a, const Band &b, int i, int t,
-                                                      bool &bad, float *terms) {
+                                                      bool &bad, float *terms, float *A = nullptr) {
   const RunDev &R = a.rd;
   const int W = b.W, H = b.H, rows = b.rows, rs = b.rowstep;
   const int ly = (int)__umulhi((unsigned)i, R.div_w), x = i - ly * W, y = b.row0 + ly;
@@ -168,7 +171,10 @@ __device__ __forceinline__ void update_general_gather(const TemporalArgs &a, con
       const unsigned row = cy == 1 ? rowU : (cy == -1 ? rowD : rowC);
       ad[k] = row + 36u * (unsigned)sx + 4u * opp_of(k);
     }
-    S[k] = ld_cluster(ad[k]);
+    if (LOCAL)
+      S[k] = A[(ad[k] - b.own_c) >> 2];
+    else
+      S[k] = ld_cluster(ad[k]);
   }
   if (in_box) store_drag_terms<false>(R, S, x, y, b.clone, terms);
   const long long n = (long long)y * W + x;
@@ -188,7 +194,10 @@ __device__ __forceinline__ void update_general_gather(const TemporalArgs &a, con
       if (ty < 0 || ty >= H) continue;
       if (tx > R.xmin && tx < R.xmax && ty > R.ymin && ty < R.ymax) continue;  // into the square
     }
-    st_cluster(ad[ok], P[k]);
+    if (LOCAL)
+      A[(ad[ok] - b.own_c) >> 2] = P[k];
+    else
+      st_cluster(ad[ok], P[k]);
   }
 }
 
@@ -410,7 +419,11 @@ __host__ __device__ inline size_t temporal_smem(int nb) {
 // the node's own (-9 / +9 floats for x -+ 1, -+ rowstep for y -+ 1).  Local
 // step: a node touches only its own nine slots, so only the box range (drag
 // terms, the interior) needs the general path.
-template <int NW, bool GATHER, bool FIELD>
+// LOCAL_BOX: box segments whose rows all lie inside the band take the
+// general gather through plain shared-memory indexing (compiled into the
+// uniform-force kernels only: in the random-field ones it raised register
+// spills).
+template <int NW, bool GATHER, bool FIELD, bool LOCAL_BOX>
 __device__ __forceinline__ void band_step(const TemporalArgs &a, const Band &b, float *A,
                                           const unsigned short *list, int nseg, const int *range,
                                           int warp, int lane, int t, const float *map, bool &bad) {
@@ -420,11 +433,17 @@ __device__ __forceinline__ void band_step(const TemporalArgs &a, const Band &b, 
   const int ngen = range[0];
   for (int k = warp; k < ngen; k += NW) {
     const int i = list[k] * 32 + lane;
+    const int ly = (int)__umulhi((unsigned)i, R.div_w);
+    const bool inner = LOCAL_BOX && __all_sync(0xffffffffu, i < b.nb && ly >= 1 && ly <= b.rows - 2);
     if (i >= b.nb) continue;
-    if (GATHER)
-      update_general_gather(a, b, i, t, bad, terms);
-    else
+    if (GATHER) {
+      if (inner)
+        update_general_gather<false, true>(a, b, i, t, bad, terms, A);
+      else
+        update_general_gather(a, b, i, t, bad, terms);
+    } else {
       update_general_local(a, b, A, i, t, bad, terms);
+    }
   }
   if (!GATHER) {
     for (int k = ngen + ((warp - ngen) & (NW - 1)); k < nseg; k += NW) {
@@ -559,14 +578,14 @@ __global__ void __launch_bounds__(THREADS, MINB) k_temporal_f32(TemporalArgs a) 
     const bool field = FIELD && t + 1 < R.field_steps;
     if ((t & 1) == 0) {
       if (field)
-        band_step<NW, true, FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
+        band_step<NW, true, FIELD, !FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
       else
-        band_step<NW, true, false>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
+        band_step<NW, true, false, !FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
     } else {
       if (field)
-        band_step<NW, false, FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
+        band_step<NW, false, FIELD, !FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
       else
-        band_step<NW, false, false>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
+        band_step<NW, false, false, !FIELD>(a, b, A, list, nseg, range, warp, lane, t, map, bad);
     }
     cluster.sync();
   }
