@@ -396,7 +396,7 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
       c->field_max_w = std::max(c->field_max_w, d.width);
       c->field_max_m1 = std::max(c->field_max_m1, M1);
       c->field_max_m2 = std::max(c->field_max_m2, M2);
-      c->field_max_tiles2 = std::max(c->field_max_tiles2, ((d.width + 15) / 16) * ((d.height + 15) / 16));
+      c->field_max_tiles2 = std::max(c->field_max_tiles2, ((d.width + 63) / 64) * ((d.height + 63) / 64));
     }
     pop += (long long)d.nclones * 9 * R.plane;
     terms += (long long)R.nterms * d.nclones;

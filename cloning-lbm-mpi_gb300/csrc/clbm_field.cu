@@ -300,72 +300,79 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
-constexpr int F2_TX = 16, F2_TY = 16, F2_KB = 64;
-constexpr int F2_LD = F2_TX + 1;  // staging row length: the 32 threads of a store spread over 16 banks
-
 // Stage 2: map[x][y] = sum over the kept columns j of Re Y[x][j] w2^(b_j y)
-// = Yr cos + Yi sin (w2^(b y) = cos - i sin), 16 x 16 outputs per CTA.
-__global__ void __launch_bounds__(F2_TX *F2_TY) k_field_stage2(FieldArgs a) {
+// = Yr cos + Yi sin (w2^(b y) = cos - i sin).  A CTA computes a 64 x 64 tile
+// of outputs, each thread a 4 x 4 register block (x = x0 + tx + 16 i,
+// y = y0 + ty + 16 j): per kept column it reads four Y values and four
+// twiddles from shared memory for sixteen outputs.  Every output still sums
+// the kept columns in their order with the same fused multiply-adds, so the
+// field is bit-identical to a one-output-per-thread loop.
+constexpr int F2_T = 64;            // outputs per tile side
+constexpr int F2_KB = 32;           // kept columns per staged chunk
+constexpr int F2_LD = F2_T + 1;     // staging row length (float2): no bank conflicts on the transposed stores
+constexpr int F2_THREADS = 256;     // 16 x 16 threads, 4 x 4 outputs each
+
+__global__ void __launch_bounds__(F2_THREADS) k_field_stage2(FieldArgs a) {
   extern __shared__ float2 sh[];
   const int g = blockIdx.y;
   const int r = field_run(a.runs, a.nruns, g);
   const RunDev &R = a.runs[r];
   if (R.field_mode == 0) return;
   const int W = R.W, H = R.H, M2 = R.M2, nb = R.fnb;
-  const int tilesx = (W + F2_TX - 1) / F2_TX;
+  const int tilesx = (W + F2_T - 1) / F2_T;
   const int tile = blockIdx.x;
-  if (tile >= tilesx * ((H + F2_TY - 1) / F2_TY)) return;
-  const int x0 = (tile % tilesx) * F2_TX, y0 = (tile / tilesx) * F2_TY;
+  if (tile >= tilesx * ((H + F2_T - 1) / F2_T)) return;
+  const int x0 = (tile % tilesx) * F2_T, y0 = (tile / tilesx) * F2_T;
   const int clone = g - R.clone_base;
-  float2 *tw = sh;             // M2 twiddles
-  float2 *Ys = sh + M2;        // [F2_KB][F2_LD]: k-major, so the 16 x of a warp read 32 consecutive words
-  int *bs = (int *)(Ys + F2_KB * F2_LD);  // the chunk's kept columns b
+  float2 *tw = sh;                    // M2 twiddles
+  float2 *Ys = tw + M2;               // [F2_KB][F2_LD]: Y of the chunk's columns, x-major rows
+  float2 *Bs = Ys + F2_KB * F2_LD;    // [F2_KB][F2_LD]: w2^(b y) of the chunk's columns
   const float2 *tw_g = a.twiddles + R.tw2_base;
-  for (int i = threadIdx.x; i < M2; i += F2_TX * F2_TY) tw[i] = tw_g[i];
+  for (int i = threadIdx.x; i < M2; i += F2_THREADS) tw[i] = tw_g[i];
   const int *blist = a.flist + R.flist_base + R.fna;
   const float *Y = (const float *)(a.ybuf + R.y_base) + (long long)clone * 2 * W * nb;  // Re rows, then Im rows
-  const int tx = threadIdx.x % F2_TX, ty = threadIdx.x / F2_TX;
-  const int x = x0 + tx, y = y0 + ty;
-  float acc = 0.f;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[i][j] = 0.f;
   for (int jb = 0; jb < nb; jb += F2_KB) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < F2_TX * F2_KB; i += F2_TX * F2_TY) {
-      const int xi = x0 + i / F2_KB, j = jb + i % F2_KB;  // coalesced along j in Y
-      const int si = (i % F2_KB) * F2_LD + i / F2_KB;
-      Ys[si] = (xi < W && j < nb) ? make_float2(Y[(long long)xi * nb + j], Y[(long long)(W + xi) * nb + j])
-                                  : make_float2(0.f, 0.f);
+    __syncthreads();  // the previous chunk is consumed (and, first time, tw is loaded)
+    for (int i = threadIdx.x; i < F2_T * F2_KB; i += F2_THREADS) {
+      const int xi = x0 + i / F2_KB, k = i % F2_KB, j = jb + k;  // coalesced along j in Y
+      Ys[k * F2_LD + i / F2_KB] = (xi < W && j < nb) ? make_float2(Y[(long long)xi * nb + j], Y[(long long)(W + xi) * nb + j])
+                                                     : make_float2(0.f, 0.f);
     }
-    for (int i = threadIdx.x; i < F2_KB; i += F2_TX * F2_TY) bs[i] = jb + i < nb ? blist[jb + i] : 0;
+    for (int i = threadIdx.x; i < F2_T * F2_KB; i += F2_THREADS) {
+      const int k = i / F2_T, yy = y0 + i % F2_T, j = jb + k;
+      Bs[k * F2_LD + i % F2_T] =
+          (j < nb && yy < H) ? tw[(int)(((unsigned)blist[j] * (unsigned)yy) % (unsigned)M2)] : make_float2(0.f, 0.f);
+    }
     __syncthreads();
-    if (x < W && y < H) {
-      // twiddle index (b y) mod M2, advanced by y along a run of consecutive
-      // kept columns (the kept columns form at most two runs)
-      const int kmax = min(F2_KB, nb - jb);
-      int prev = -2, idx = 0;
-      if (nb == M2) {  // every column kept: b = jb + k
-        idx = (int)(((unsigned)jb * (unsigned)y) % (unsigned)M2);
-        for (int k = 0; k < kmax; k++) {
-          const float2 t = tw[idx], v = Ys[k * F2_LD + tx];
-          acc = fmaf(v.x, t.x, fmaf(-v.y, t.y, acc));
-          idx += y;
-          if (idx >= M2) idx -= M2;
-        }
-      } else
-      for (int k = 0; k < kmax; k++) {
-        const int b = bs[k];
-        if (b == prev + 1) {
-          idx += y;
-          if (idx >= M2) idx -= M2;
-        } else {
-          idx = (int)(((unsigned)b * (unsigned)y) % (unsigned)M2);
-        }
-        prev = b;
-        const float2 t = tw[idx], v = Ys[k * F2_LD + tx];
-        acc = fmaf(v.x, t.x, fmaf(-v.y, t.y, acc));
-      }
+    const int kmax = min(F2_KB, nb - jb);
+    for (int k = 0; k < kmax; k++) {
+      float2 v[4], t[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) v[i] = Ys[k * F2_LD + tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; j++) t[j] = Bs[k * F2_LD + ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = fmaf(v[i].x, t[j].x, fmaf(-v[i].y, t[j].y, acc[i][j]));
     }
   }
-  if (x < W && y < H) a.maps[R.map_base + (long long)clone * W * H + (long long)y * W + x] = acc;
+  float *map = a.maps + R.map_base + (long long)clone * W * H;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int y = y0 + ty + 16 * j;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int x = x0 + tx + 16 * i;
+      if (x < W && y < H) map[(long long)y * W + x] = acc[i][j];
+    }
+  }
 }
 
 cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int max_m1, int max_m2,
@@ -378,9 +385,9 @@ cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int m
   k_field_stage1_tc<<<total_clones, tc::THREADS, tc::SMEM, s>>>(a);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const size_t sh2 = sizeof(float2) * ((size_t)max_m2 + F2_LD * F2_KB) + sizeof(int) * F2_KB;
+  const size_t sh2 = sizeof(float2) * ((size_t)max_m2 + 2 * F2_LD * F2_KB);
   dim3 g2(max_tiles2, total_clones);
-  k_field_stage2<<<g2, F2_TX * F2_TY, sh2, s>>>(a);
+  k_field_stage2<<<g2, F2_THREADS, sh2, s>>>(a);
   return cudaGetLastError();
 }
 
