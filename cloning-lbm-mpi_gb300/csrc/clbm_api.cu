@@ -390,7 +390,7 @@ extern "C" int clbm_create(const clbm_run_desc *runs, int nruns, int precision, 
         h_tw[tw + M1 + k] = make_float2((float)std::cos(2.0 * M_PI * k / M2), (float)-std::sin(2.0 * M_PI * k / M2));
       spec += (long long)na * nb;
       tw += M1 + M2;
-      ybuf += (long long)d.nclones * d.width * nb;
+      ybuf += (long long)d.nclones * d.width * field_y_pitch(nb);
       maps += (long long)d.nclones * R.nodes;
       c->any_field = true;
       c->field_max_w = std::max(c->field_max_w, d.width);

@@ -191,7 +191,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
   const unsigned tmem = tmem_base_s;
   const float *spec = a.spec + R.spec_base;
   const float *dft = a.dft + R.fa_base;
-  float *Yr = (float *)(a.ybuf + R.y_base) + (long long)clone * 2 * W * nb, *Yi = Yr + (long long)W * nb;
+  const int nbp = field_y_pitch(nb);  // row pitch of Y
+  float *Yr = (float *)(a.ybuf + R.y_base) + (long long)clone * 2 * W * nbp, *Yi = Yr + (long long)W * nbp;
   const int ntiles_m = R.f_mpad / MT, passes = (ntiles_m + TILES - 1) / TILES;
   const int ntiles_n = (nb + NT - 1) / NT, nchunks = R.f_kchunks;
   int gc = 0;          // chunks issued by this CTA so far (buffer and mbarrier phase)
@@ -273,7 +274,10 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
     static_assert(THREADS == 512, "16 warps: 4 lane quarters x 4 column quarters");
     for (int t = 0; t < tiles; t++) {
       const int m = (pass * TILES + t) * MT + 32 * q + lane;
-      float *dst = m < W ? Yr + (long long)m * nb : (m < 2 * W ? Yi + (long long)(m - W) * nb : nullptr);
+      float *dst = m < W ? Yr + (long long)m * nbp : (m < 2 * W ? Yi + (long long)(m - W) * nbp : nullptr);
+      // columns of this tile inside the padded row (the padding takes the
+      // accumulators of the empty columns, zeros)
+      const int ncols_p = min(NT, nbp - nt * NT);
 #pragma unroll
       for (int j = 0; j < 2; j++) {
         const int n0 = 32 * h + 16 * j;
@@ -281,8 +285,9 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_field_stage1_tc(FieldArgs a)
         tmem_ld16(tmem + ((unsigned)(32 * q) << 16) + t * NT + n0, v);
         if (dst) {
 #pragma unroll
-          for (int i = 0; i < 16; i++)
-            if (n0 + i < ncols) dst[nt * NT + n0 + i] = v[i];
+          for (int i = 0; i < 4; i++)
+            if (n0 + 4 * i + 3 < ncols_p)
+              *(float4 *)(dst + nt * NT + n0 + 4 * i) = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
         }
       }
     }
@@ -330,7 +335,8 @@ __global__ void __launch_bounds__(F2_THREADS) k_field_stage2(FieldArgs a) {
   const float2 *tw_g = a.twiddles + R.tw2_base;
   for (int i = threadIdx.x; i < M2; i += F2_THREADS) tw[i] = tw_g[i];
   const int *blist = a.flist + R.flist_base + R.fna;
-  const float *Y = (const float *)(a.ybuf + R.y_base) + (long long)clone * 2 * W * nb;  // Re rows, then Im rows
+  const int nbp = field_y_pitch(nb);
+  const float *Y = (const float *)(a.ybuf + R.y_base) + (long long)clone * 2 * W * nbp;  // Re rows, then Im rows
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   float acc[4][4];
 #pragma unroll
@@ -341,7 +347,7 @@ __global__ void __launch_bounds__(F2_THREADS) k_field_stage2(FieldArgs a) {
     __syncthreads();  // the previous chunk is consumed (and, first time, tw is loaded)
     for (int i = threadIdx.x; i < F2_T * F2_KB; i += F2_THREADS) {
       const int xi = x0 + i / F2_KB, k = i % F2_KB, j = jb + k;  // coalesced along j in Y
-      Ys[k * F2_LD + i / F2_KB] = (xi < W && j < nb) ? make_float2(Y[(long long)xi * nb + j], Y[(long long)(W + xi) * nb + j])
+      Ys[k * F2_LD + i / F2_KB] = (xi < W && j < nb) ? make_float2(Y[(long long)xi * nbp + j], Y[(long long)(W + xi) * nbp + j])
                                                      : make_float2(0.f, 0.f);
     }
     for (int i = threadIdx.x; i < F2_T * F2_KB; i += F2_THREADS) {

@@ -151,6 +151,9 @@ cudaError_t launch_fields(const FieldArgs &a, int total_clones, int max_w, int m
 // mpad * 32 * kchunks floats
 inline int field_dft_mpad(int W) { return (2 * W + 127) / 128 * 128; }
 inline int field_dft_kchunks(int na) { return (2 * na + 31) / 32; }
+// row pitch (floats) of the stage-1 output Y of nb kept columns: a multiple of
+// 4, so a row starts on a 16-byte boundary and the stores are 16-byte vectors
+__host__ __device__ inline int field_y_pitch(int nb) { return (nb + 3) & ~3; }
 void build_field_dft_image(int W, int M1, const int *alist, int na, int mpad, int kchunks, float *out);
 // cluster-resident interval kernel (clbm_temporal.cu): launch with the bands
 // of a.band_row0; resident clusters of a shape whose largest band has
