@@ -17,7 +17,8 @@
 // Box-Muller.  The field is stored as FP32 in the populations' node order
 // y*W + x.
 //
-// Stage 1 carries 97 % of the arithmetic and runs on the tensor cores
+// Stage 1 carries most of the arithmetic (83 % of the multiply-adds for the
+// reference's sigma = 32 on a 256 x 64 lattice) and runs on the tensor cores
 // (tcgen05, TF32 operands, FP32 accumulation in tensor memory): per clone a
 // real GEMM D = A B with
 //   rows    m = (part, x): Re Y[x] for m < W, Im Y[x] for W <= m < 2W
@@ -43,8 +44,9 @@
 // move the field by under 3e-6 of its RMS).  The sums over a and b above run
 // over the kept lists; every kept mode draws its normal from the same Philox
 // counter (a M2 + b, clone, interval, run) as in the full transform.  For the
-// reference's sigma = 32 on a 256 x 64 lattice this keeps 43 of 511 rows and
-// 11 of 127 columns.
+// reference's sigma = 32 on a 256 x 64 lattice this keeps 158 of 511 rows and
+// all 127 columns (the periodised Gaussian is wide against the 127-column
+// period).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
