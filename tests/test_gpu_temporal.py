@@ -249,3 +249,29 @@ def test_fused_reseed_equals_streaming(gpu, clbm_lib, orc, W, H, side, xc, yc, c
     assert any(not np.array_equal(out[0][i], np.arange(nc)) for i in (1, 4, 7))
     for a, b in zip(*out):
         assert np.array_equal(a, b)
+
+
+def test_fused_reseed_two_runs(gpu, clbm_lib, orc):
+    """Two cluster-resident runs of different lattices in one context (each
+    interval kernel forms its own run's P_0, run index and clone base
+    included): bit-identical to both runs streaming."""
+    u0, T = 0.05, 20
+    descs = []
+    for (W, H, side, xc, yc, nc, seed) in ((64, 24, 6, 16, 12, 5, 3), (96, 23, 5, 30, 9, 4, 4)):
+        g = orc.channel_geom(W, H, side, xc, yc)
+        descs.append(clbm_lib.RunDesc(width=g.nx, height=g.ny, xmin=g.xmin, xmax=g.xmax, ymin=g.ymin, ymax=g.ymax,
+                                      nclones=nc, ranks=1, tau=0.57, beta=side * u0 * u0 / ((W - 1) * (H - 1)),
+                                      alpha=12.0, force_scale=2 / (u0 * u0 * side), dt=u0 / side,
+                                      perturb_mode=clbm_lib.PERTURB_UNIFORM, eps=1e-3, seed=seed))
+    out = []
+    for variants in ([4, 4], [temporal_variant(2, 0), temporal_variant(3, 1)]):
+        with clbm_lib.Sampler(descs, clbm_lib.FP32, max_steps=T, flags=clbm_lib.FLAG_GRAPH) as s:
+            s.set_run_variants(variants)
+            for r in range(2):
+                s.init_equilibrium(r, u0, 1e-3, 7 + r)
+            rv = s.run_sampler(T, 3)
+            res = [rv] + [s.dump(r, j) for r in range(2) for j in range(descs[r].nclones)]
+            assert s.error_word() == 0
+            out.append(res)
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
