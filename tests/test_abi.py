@@ -54,3 +54,18 @@ def test_no_device_means_status_not_fallback(clbm_lib):
     ok = clbm_lib.RunDesc(width=16, height=8, xmin=4, xmax=6, ymin=2, ymax=4, nclones=2, ranks=1, tau=0.6)
     h = C.c_void_p()
     assert clbm_lib.lib().clbm_create(C.byref(ok), 1, 0, 10, 0, C.byref(h)) == clbm_lib.ERR_CUDA
+
+
+def test_variant_numbering(clbm_lib):
+    """The autotuner's variant numbers: 8 streaming launch shapes, then the
+    cluster-resident kernel per cluster size (1, 2, 4, 8, 16, 3, 5, 6, 7, 9,
+    10, in that order: the sizes that are not powers of two appended) times
+    three thread counts (the numbering include/clbm.h documents)."""
+    assert clbm_lib.describe_variant(7) == {"kind": "streaming", "kernel": "k_step_f32", "variant": 7}
+    sizes = (1, 2, 4, 8, 16, 3, 5, 6, 7, 9, 10)
+    for q, cs in enumerate(sizes):
+        for tv, threads in enumerate((1024, 512, 256)):
+            d = clbm_lib.describe_variant(8 + 3 * q + tv)
+            assert (d["kind"], d["cluster_size"], d["threads"]) == ("cluster-resident", cs, threads)
+    assert clbm_lib.describe_variant(14)["cluster_size"] == 4  # the powers of two keep their numbers
+    assert clbm_lib.describe_variant(23)["cluster_size"] == 3
